@@ -1,0 +1,132 @@
+"""Pins the CPU oracle (restated kbw Dense<F>) against the golden fixtures made
+by the independent numpy model and against closed-form known answers."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from kbw_gb300 import circuits as C
+from conftest import decode_circuit, load_golden, rel_err
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_random_small_circuits(prec, tol):
+    g = load_golden("random_small.npz")
+    for i in range(int(g["count"])):
+        n = int(g["c%d_n" % i])
+        o = oracle.OracleDense(n, prec)
+        o.apply(decode_circuit(g, "c%d" % i))
+        assert rel_err(o.state(), g["c%d_state" % i]) < tol, (prec, i)
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 1e-4)])
+def test_grover_probabilities(prec, tol):
+    g = load_golden("grover12.npz")
+    for seed in range(3):
+        m = C.grover_marked(seed)
+        assert m == int(g["marked"][seed])
+        o = oracle.OracleDense(12, prec)
+        o.apply(C.grover(12, m, 50))
+        prob = np.abs(o.state()) ** 2
+        assert np.max(np.abs(prob - g["prob_seed%d" % seed])) < tol
+        assert abs(prob[m] - C.grover_success_probability(12, 50)) < tol
+
+
+def test_grover_samples_bit_exact():
+    g = load_golden("grover12.npz")
+    o = oracle.OracleDense(12, "c128")
+    o.apply(C.grover(12, C.grover_marked(0), 50))
+    st, ct = o.sample(list(range(12)), 1024, g["sample_draws"])
+    assert np.array_equal(st, g["sample_states"]) and np.array_equal(ct, g["sample_counts"])
+
+
+def test_measure_and_sample_with_draws():
+    g = load_golden("measure.npz")
+    for i in range(int(g["count"])):
+        n = int(g["m%d_n" % i])
+        qubits = [int(q) for q in g["m%d_qubits" % i]]
+        o = oracle.OracleDense(n, "c128")
+        o.apply(decode_circuit(g, "m%d" % i))
+        st, ct = o.sample(qubits, 256, g["m%d_sdraws" % i])
+        assert np.array_equal(st, g["m%d_sstates" % i]) and np.array_equal(ct, g["m%d_scounts" % i])
+        res = o.measure(qubits, g["m%d_draws" % i])
+        assert res == int(g["m%d_result" % i])
+        assert rel_err(o.state(), g["m%d_post" % i]) < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-5)])
+def test_exp_value(prec, tol):
+    g = load_golden("expval.npz")
+    for i in range(int(g["count"])):
+        n, L = int(g["e%d_n" % i]), int(g["e%d_L" % i])
+        o = oracle.OracleDense(n, prec)
+        o.apply(C.hea(n, L, g["e%d_params" % i]))
+        assert abs(o.exp_value(C.tfim_ring(n)) - float(g["e%d_tfim" % i])) < tol * n
+        ham_y = [(0.7, [(C.PAULI_Y, 0), (C.PAULI_X, n - 1)]), (-1.3, [(C.PAULI_Y, 1)]),
+                 (0.25, [(C.PAULI_Z, 2), (C.PAULI_Y, 3), (C.PAULI_X, 0)]), (2.0, [])]
+        assert abs(o.exp_value(ham_y) - float(g["e%d_mixed" % i])) < tol * 10
+
+
+def test_ghz_and_rotation_kats():
+    o = oracle.OracleDense(5, "c128")
+    o.hadamard(0)
+    for q in range(4):
+        o.pauli_x(q + 1, [q])
+    st, re, im = o.dump(list(range(5)))
+    assert list(st) == [0, 31]
+    assert np.allclose(re, [1 / math.sqrt(2)] * 2) and np.allclose(im, 0)
+    for theta in (0.3, 1.7, -2.2):
+        o = oracle.OracleDense(1, "c128")
+        o.ry(theta, 0)
+        assert abs(o.exp_value([(1.0, [(C.PAULI_Z, 0)])]) - math.cos(theta)) < 1e-14
+        o = oracle.OracleDense(1, "c128")
+        o.rx(theta, 0)
+        assert abs(o.exp_value([(1.0, [(C.PAULI_Y, 0)])]) + math.sin(theta)) < 1e-14
+
+
+def test_gate_inverse_identity_and_norm():
+    n = 6
+    g = C.random_circuit(n, 60, 7, max_controls=2)
+    o = oracle.OracleDense(n, "c128")
+    o.apply(g)
+    assert abs(np.linalg.norm(o.state()) - 1.0) < 1e-13
+    inv = []
+    for kind, t, c, a in reversed(g):
+        if kind in (C.P, C.RX, C.RY, C.RZ):
+            inv.append((kind, t, c, -a))
+        else:
+            inv.append((kind, t, c, a))
+    o.apply(inv)
+    ref = np.zeros(1 << n, complex)
+    ref[0] = 1
+    assert rel_err(o.state(), ref) < 1e-13
+
+
+def test_swap_relabel_invariance():
+    """Swapping qubits a,b, applying the gate list with a,b exchanged and
+    swapping back equals the flat run (the Block wrapper's contract)."""
+    n = 6
+    g = C.random_circuit(n, 40, 9, max_controls=2)
+    flat = oracle.OracleDense(n, "c128")
+    flat.apply(g)
+    a, b = 1, 5
+    swap = {a: b, b: a}
+    o = oracle.OracleDense(n, "c128")
+    o.swap_qubits(a, b)
+    o.apply([(k, swap.get(t, t), tuple(swap.get(c, c) for c in cs), ang) for k, t, cs, ang in g])
+    o.swap_qubits(a, b)
+    assert rel_err(o.state(), flat.state()) < 1e-14
+
+
+def test_weighted_index_rule():
+    assert oracle.uniform_scale(1.0) == 1.0
+    # every double in [1, 2) keeps its scale (max draw * scale stays below it)
+    for t in (1.5, 1.9999999999999998, 0.75, 3.0):
+        s = oracle.uniform_scale(t)
+        assert s <= t and s * (1 - 2.0 ** -52) < t
+
+
+def test_too_many_qubits_rejected():
+    with pytest.raises(ValueError):
+        oracle.OracleDense(33, "c64")
