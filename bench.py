@@ -1,0 +1,372 @@
+"""Benchmark of the dense state-vector hot path on GB300.
+
+Workload (one step): the seeded 30-qubit random brickwork circuit, 20 layers
+(600 one-qubit gates from {H,X,Y,Z,S,T,RX,RY,RZ} + 290 CNOTs), applied to the
+resident complex128 state (16 GiB, far larger than the 129 MB L2, so no L2
+flush is needed between steps).  The same circuit in complex64 is reported
+as a secondary line item.
+
+value: gate-equivalent GB/s = gates x (2 x 16 B x 2^30) / step time, i.e. the
+bytes a one-gate-per-sweep engine (the reference Dense) would move.
+roofline: the fused sweep kernel's algorithmic bytes per launch (one full
+read + write of the state) over its CUDA-event-timed launch duration, against
+the measured HBM copy bandwidth.
+e2e: the same metric through the C ABI with host buffers: per step the state
+is cleared, every gate is submitted by its own trait call, then <Z_i> for all
+qubits and one full-register measurement (host draws) are read back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "30q gate GB/s vs HBM peak; adjoint vs param-shift grads/s at <=1e-5 err"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_port_rate(n, prec, gates, budget_s, threads=None):
+    """Time the restated Dense<F> (oracle, OpenMP) on the first gates of the
+    workload until `budget_s` of CPU work; returns (gate-eq GB/s, info)."""
+    import oracle
+    if threads:
+        oracle.set_num_threads(threads)
+    o = None
+    for nn in (n, n - 1, n - 2):
+        try:
+            o = oracle.OracleDense(nn, prec)
+            n_used = nn
+            break
+        except ValueError:
+            continue
+    if o is None:
+        return None, {"sample": "host allocation failed"}
+    B = 16 if prec == "c128" else 8
+    done, t0 = 0, time.perf_counter()
+    while done < len(gates):
+        kind, t, c, a = gates[done]
+        if t >= n_used or any(q >= n_used for q in c):
+            done += 1
+            continue
+        o.gate(kind, t, c, a)
+        done += 1
+        if time.perf_counter() - t0 > budget_s and done >= 2:
+            break
+    dt = time.perf_counter() - t0
+    rate = done * 2 * B * (1 << n_used) / dt / 1e9
+    return rate, {"gates": done, "qubits": n_used, "seconds": round(dt, 3), "threads": oracle.num_threads()}
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU Dense path, as the oracle port (the Rust crate
+    cannot be built here): each step applies a bounded slice of the same
+    brickwork circuit at 30 qubits with every host thread."""
+    if rank != 0:
+        return
+    from kbw_gb300 import circuits as C
+    import oracle
+    n, prec = args.qubits, args.prec
+    circ = C.brickwork(n, args.layers, 0)
+    o = oracle.OracleDense(n, prec)
+    B = 16 if prec == "c128" else 8
+    per_step = args.ref_gates
+    pos = 0
+
+    def step():
+        nonlocal pos
+        for _ in range(per_step):
+            kind, t, c, a = circ[pos % len(circ)]
+            o.gate(kind, t, c, a)
+            pos += 1
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = args.steps * per_step * 2 * B * (1 << n) / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == "c128" else "f32", "data": "synthetic",
+        "config": {"workload": "brickwork-%dq-%dlayers-%s" % (n, args.layers, prec), "qubits": n,
+                   "precision": prec, "gates_per_step": per_step},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": "%d gates per step of the %dq brickwork, restated Dense<f64> (OpenMP)"
+                                   % (per_step, n)},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import kbw_gb300
+    from kbw_gb300 import DenseGB300
+    from kbw_gb300 import circuits as C
+    from kbw_gb300 import _native as N
+
+    kbw_gb300.load()
+    torch.cuda.set_device(local)
+    N.select_device(local)
+    n, prec = args.qubits, args.prec
+    B = 16 if prec == "c128" else 8
+    circ = C.brickwork(n, args.layers, 0)
+    G = len(circ)
+    step_bytes = G * 2 * B * (1 << n)
+
+    sim = DenseGB300(n, prec)
+    ext = torch.cuda.ExternalStream(sim.stream_handle())
+
+    def step():
+        sim.apply(circ)
+        sim.flush()
+
+    for _ in range(args.warmup):
+        step()
+    _, passes = sim.last_flush_stats()
+    sim.profile(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    barrier(world)
+    l0 = N.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(args.steps):
+        step()
+    e1.record(ext)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    launches = N.launch_count() - l0
+    clk = clocks.stop()
+    nl, kms, kbytes = sim.profile_read()
+    sim.profile(False)
+    ms = max_over_ranks(world, ms)
+    ms_step = ms / args.steps
+    value = world * step_bytes / (ms_step * 1e-3) / 1e9
+
+    peak, peak_kind = load_peaks()
+    achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else None
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None, "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                "traffic": args.traffic, "kernel": "k_sweep<%s>" % ("double" if prec == "c128" else "float"),
+                "launches": nl, "avg_launch_ms": round(kms / max(nl, 1), 4), "peak_source": peak_kind + " hbm_gbs"}
+
+    # ---- e2e through the C ABI, host buffers ----
+    zs = [(1.0, [(C.PAULI_Z, q)]) for q in range(n)]
+    calls = {C.X: sim.pauli_x, C.Y: sim.pauli_y, C.Z: sim.pauli_z, C.H: sim.hadamard,
+             C.P: sim.phase, C.RX: sim.rx, C.RY: sim.ry, C.RZ: sim.rz}
+
+    def e2e_step(seed):
+        sim.clear()
+        for kind, t, c, a in circ:
+            if kind in C.PARAMETRIC:
+                calls[kind](a, t, c)
+            else:
+                calls[kind](t, c)
+        ez = sim.exp_value(zs)
+        bits = sim.measure(list(range(n)), C.uniform_draws(n, seed))
+        return ez, bits
+
+    e2e_step(0)
+    torch.cuda.synchronize()
+    h0, d0 = N.transfer_bytes()
+    t0 = time.perf_counter()
+    for s in range(args.e2e_steps):
+        e2e_step(s + 1)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / args.e2e_steps)
+    h1, d1 = N.transfer_bytes()
+    e2e = {"value": round(world * step_bytes / e2e_s / 1e9, 1), "unit": "GB/s",
+           "h2d_bytes_per_step": (h1 - h0) // args.e2e_steps, "d2h_bytes_per_step": (d1 - d0) // args.e2e_steps,
+           "ms_per_step": round(e2e_s * 1e3, 2),
+           "calls": "clear + %d gate calls + exp_value(%d Z_i) + measure(%d qubits)" % (G, n, n)}
+    sim.close()
+    del sim
+
+    # ---- secondary: the same circuit in complex64 ----
+    secondary = {}
+    if args.secondary and prec == "c128":
+        s64 = DenseGB300(n, "c64")
+        for _ in range(2):
+            s64.apply(circ)
+            s64.flush()
+        s64.profile(True)
+        ext64 = torch.cuda.ExternalStream(s64.stream_handle())
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(ext64)
+        for _ in range(args.steps):
+            s64.apply(circ)
+            s64.flush()
+        a1.record(ext64)
+        torch.cuda.synchronize()
+        ms64 = a0.elapsed_time(a1) / args.steps
+        nl64, kms64, kb64 = s64.profile_read()
+        ach64 = kb64 / (kms64 * 1e-3) / 1e9
+        secondary["c64"] = {"value": round(G * 2 * 8 * (1 << n) / (ms64 * 1e-3) / 1e9, 1), "unit": "GB/s",
+                            "ms_per_step": round(ms64, 3), "sweeps_per_step": s64.last_flush_stats()[1],
+                            "roofline": {"achieved": round(ach64, 1), "frac": round(ach64 / peak, 4),
+                                         "avg_launch_ms": round(kms64 / max(nl64, 1), 4)}}
+        s64.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, info = cpu_port_rate(n, prec, circ, args.cpu_seconds)
+        if rate is not None:
+            cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": info.get("threads"), "kind": "port",
+                   "sample": "first %d gates of the %dq brickwork on the restated Dense<%s> (OpenMP), %.1f s"
+                             % (info["gates"], info["qubits"], "f64" if prec == "c128" else "f32", info["seconds"])}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == "c128" else "f32",
+            "data": "synthetic: seeded random brickwork circuit (numpy default_rng(0))",
+            "config": {"workload": "brickwork-%dq-%dlayers-%s" % (n, args.layers, prec), "qubits": n,
+                       "layers": args.layers, "gates": G, "precision": prec, "sweeps_per_step": passes,
+                       "l2": "state %d GiB > 129 MB L2; no flush needed" % ((B << n) >> 30),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "sweep_gbs": round(world * passes * 2 * B * (1 << n) / (ms_step * 1e-3) / 1e9, 1),
+            "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        }
+        line.update(secondary)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--layers", type=int, default=20)
+    ap.add_argument("--prec", choices=["c64", "c128"], default="c128")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-gates", type=int, default=4)
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per sweep launch, when known")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

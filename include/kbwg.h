@@ -1,0 +1,216 @@
+/*
+ * kbwg.h -- C ABI of the GB300 dense state-vector engine ("densegb300").
+ *
+ * The engine is a drop-in backend for the Ket Bitwise Simulator's dense path.
+ * Each entry point below replaces one method of the reference's backend trait
+ * `QuantumExecution` (kbw src/quantum_execution.rs:48-162) or one piece of the
+ * `QubitManager` adapter built on it (src/quantum_execution.rs:171-427); the
+ * citation is given per entry.  A Rust `QuantumExecution` impl binds these
+ * symbols one to one, exactly as the reference's
+ * `kbw_make_configuration` (kbw.h:48-54, src/c_api.rs:60-129) binds its own
+ * backends.
+ *
+ * Conventions
+ *  - Every function returns an int32 status: KBWG_OK (0) or a KBWG_E* code.
+ *    No C++ exception or CUDA error crosses this boundary; the text of the
+ *    last error on the calling thread is available from kbwg_last_error().
+ *  - Qubit indices and counts are uintptr_t (the reference's usize).  Bit q
+ *    of a basis-state index is qubit q, as in the reference (src/bitwise.rs).
+ *  - Angles and probabilities are double, as in the trait.
+ *  - A handle owns one state vector on one GPU (the device current when it
+ *    was created) and one CUDA stream.  Use a handle from one host thread at
+ *    a time (the trait's `&mut self`).  Gate calls are queued on the host and
+ *    executed by fused kernels at the next call that reads the state.
+ *  - Host buffers are plain pointers; nothing here takes torch types.
+ */
+#ifndef KBWG_H_INCLUDED
+#define KBWG_H_INCLUDED
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kbwg_sim kbwg_sim;
+
+/* status codes (KetError analogues; 0 = Success) */
+enum {
+    KBWG_OK = 0,
+    KBWG_EINVAL = 1,    /* bad argument: qubit index, null pointer, size */
+    KBWG_EQUBITS = 2,   /* num_qubits out of range: KetError::ExecutionFailed in src/dense.rs:71-73 */
+    KBWG_ENOMEM = 3,    /* device or pinned-host allocation failed */
+    KBWG_ECUDA = 4,     /* a CUDA runtime call failed */
+    KBWG_EWEIGHT = 5,   /* all sampling weights are zero (src/convert.rs:60 panics) */
+    KBWG_ECAPACITY = 6, /* caller buffer too small; *size holds the size needed */
+    KBWG_ETIMEOUT = 7,  /* a bounded device-side wait ran out */
+    KBWG_EUNSUPPORTED = 8
+};
+
+/* amplitude precision: complex64 (Dense<f32>, the reference default alias,
+ * src/lib.rs:130) or complex128 (Dense<f64>) */
+enum { KBWG_C64 = 0, KBWG_C128 = 1 };
+
+/* gate kinds, in trait order (src/quantum_execution.rs:58-79) */
+enum {
+    KBWG_X = 0, KBWG_Y = 1, KBWG_Z = 2, KBWG_H = 3,
+    KBWG_P = 4, KBWG_RX = 5, KBWG_RY = 6, KBWG_RZ = 7
+};
+
+/* Pauli codes of ket Hamiltonian terms (ket::ir::hamiltonian::Pauli) */
+enum { KBWG_PAULI_X = 1, KBWG_PAULI_Y = 2, KBWG_PAULI_Z = 3 };
+
+/* creation flags */
+enum {
+    KBWG_FLAG_NO_FUSION = 1u << 0, /* run one kernel per gate (debug / A-B timing) */
+    KBWG_FLAG_FAST_C128 = 1u << 1, /* complex128 gate arithmetic in float-float (see DESIGN) */
+    KBWG_FLAG_EXACT_ORDER = 1u << 2 /* fuse without reordering commuting gates: amplitudes then
+                                       equal the reference's bit for bit */
+};
+
+/* QuantumExecution::new (src/quantum_execution.rs:53; src/dense.rs:70-89).
+ * Allocates 2^num_qubits amplitudes in |0...0>.  num_qubits must be <= 32
+ * (KBWG_EQUBITS otherwise, as Dense::new). */
+int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_sim **out);
+
+/* Drop of the backend (ket frees its QPUConfig, src/c_api.rs:124). */
+int32_t kbwg_free(kbwg_sim *sim);
+
+/* QuantumExecution::pauli_x/pauli_y/pauli_z/hadamard
+ * (src/quantum_execution.rs:58-67; src/dense.rs:91-209). */
+int32_t kbwg_pauli_x(kbwg_sim *sim, uintptr_t target, const uintptr_t *control, uintptr_t n_control);
+int32_t kbwg_pauli_y(kbwg_sim *sim, uintptr_t target, const uintptr_t *control, uintptr_t n_control);
+int32_t kbwg_pauli_z(kbwg_sim *sim, uintptr_t target, const uintptr_t *control, uintptr_t n_control);
+int32_t kbwg_hadamard(kbwg_sim *sim, uintptr_t target, const uintptr_t *control, uintptr_t n_control);
+
+/* QuantumExecution::phase/rx/ry/rz (src/quantum_execution.rs:70-79;
+ * src/dense.rs:211-334). */
+int32_t kbwg_phase(kbwg_sim *sim, double lambda, uintptr_t target, const uintptr_t *control,
+                   uintptr_t n_control);
+int32_t kbwg_rx(kbwg_sim *sim, double theta, uintptr_t target, const uintptr_t *control,
+                uintptr_t n_control);
+int32_t kbwg_ry(kbwg_sim *sim, double theta, uintptr_t target, const uintptr_t *control,
+                uintptr_t n_control);
+int32_t kbwg_rz(kbwg_sim *sim, double theta, uintptr_t target, const uintptr_t *control,
+                uintptr_t n_control);
+
+/* One gate record for kbwg_apply_gates: controls as a bit mask. */
+typedef struct kbwg_gate {
+    uint32_t kind;   /* KBWG_X .. KBWG_RZ */
+    uint32_t target; /* qubit index */
+    uint64_t control_mask;
+    double angle;    /* ignored for X, Y, Z, H */
+} kbwg_gate;
+
+/* A gate list in one call: LiveExecution::compute_gate per element
+ * (src/quantum_execution.rs:310-314, 251-270). */
+int32_t kbwg_apply_gates(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates);
+
+/* QuantumExecution::measure_p1 (src/quantum_execution.rs:84; src/dense.rs:336-352).
+ * FP64 on-device reduction; does not collapse. */
+int32_t kbwg_measure_p1(kbwg_sim *sim, uintptr_t target, double *p1);
+
+/* QuantumExecution::measure_collapse (src/quantum_execution.rs:90;
+ * src/dense.rs:354-367): keep amplitudes whose bit `target` equals `result`,
+ * scaled by p (= 1/sqrt(P(result))), zero the rest. */
+int32_t kbwg_measure_collapse(kbwg_sim *sim, uintptr_t target, bool result, double p);
+
+/* QubitManager::do_measure (src/quantum_execution.rs:272-292): measure the
+ * listed qubits one at a time, last listed first, with one uniform draw in
+ * [0,1) per qubit taken from `draws` in that order (the reference draws
+ * these from its StdRng).  draws == NULL uses the handle's own generator
+ * (seeded from KBW_SEED).  *result packs qubits[0] as the most significant
+ * bit. */
+int32_t kbwg_measure(kbwg_sim *sim, const uintptr_t *qubits, uintptr_t n_qubits,
+                     const double *draws, uint64_t *result);
+
+/* QuantumExecution::dump (src/quantum_execution.rs:93; src/dense.rs:369-397):
+ * basis states with |a| > eps (1e-6 for c64, 1e-15 for c128), in index
+ * order, re-packed with qubits[0] as the most significant bit.  Two-call
+ * protocol: with capacity smaller than the support, fills nothing, sets
+ * *size and returns KBWG_ECAPACITY (pass capacity 0 to query). */
+int32_t kbwg_dump(kbwg_sim *sim, const uintptr_t *qubits, uintptr_t n_qubits,
+                  uint64_t *basis_states, double *re, double *im, uintptr_t capacity,
+                  uintptr_t *size);
+
+/* QuantumExecution::sample default (src/quantum_execution.rs:99-102) with
+ * src/convert.rs:30-73: `shots` draws u_k in [0,1) (NULL: the handle's
+ * generator) pick basis states by WeightedIndex over the support.  Writes
+ * the histogram sorted by packed basis state; *n_out = number of distinct
+ * states.  capacity must be >= min(shots, 2^n_qubits). */
+int32_t kbwg_sample(kbwg_sim *sim, const uintptr_t *qubits, uintptr_t n_qubits, uintptr_t shots,
+                    const double *draws, uint64_t *states, uint64_t *counts, uintptr_t capacity,
+                    uintptr_t *n_out);
+
+/* QuantumExecution::exp_value (src/quantum_execution.rs:104-158): sum over
+ * Pauli strings of coefficient * <psi|P|psi>, computed directly on the GPU
+ * (no basis rotations, FP64 accumulation).  String k has terms
+ * [offsets[k], offsets[k+1]) of paulis[] / qubits[]. */
+int32_t kbwg_exp_value(kbwg_sim *sim, const uint8_t *paulis, const uintptr_t *qubits,
+                       const uintptr_t *offsets, const double *coefficients, uintptr_t n_strings,
+                       double *out);
+
+/* QuantumExecution::clear (src/quantum_execution.rs:161; src/dense.rs:399-406). */
+int32_t kbwg_clear(kbwg_sim *sim);
+
+/* Execute queued gates now and wait for the device. */
+int32_t kbwg_flush(kbwg_sim *sim);
+
+/* Raw amplitude access (interleaved re,im in the handle's precision). */
+int32_t kbwg_get_state(kbwg_sim *sim, void *host_dst, uintptr_t bytes);
+int32_t kbwg_set_state(kbwg_sim *sim, const void *host_src, uintptr_t bytes);
+int32_t kbwg_state_info(kbwg_sim *sim, uintptr_t *num_qubits, int32_t *precision,
+                        void **device_ptr, uintptr_t *bytes);
+
+/* BlockSimulator::swap (src/block.rs:41-53; src/dense_v2.rs:360-396;
+ * GPU in_place_swap src/dense_gpu/kernel.rs:437-466), flat-index form:
+ * exchange physical qubits a and b with one in-place permutation pass. */
+int32_t kbwg_swap_qubits(kbwg_sim *sim, uintptr_t a, uintptr_t b);
+
+/* kbw_build_info (kbw.h:64; src/c_api.rs:149-163). */
+int32_t kbwg_build_info(const uint8_t **msg, uintptr_t *size);
+
+/* ---- diagnostics (no counterpart in the reference) ---------------------- */
+
+/* Run the fusion planner on the host for a gate list (no GPU needed) and
+ * report how the engine would execute it: order[] receives the gate indices
+ * in execution order, sweep_end[k] the end (exclusive) in order[] of sweep k,
+ * tile_mask[k] the qubits of sweep k's tile.  The arrays need n_gates
+ * entries.  With precision KBWG_C64 tiles have 13 qubits, with KBWG_C128 12;
+ * num_qubits must be at least that.  flags: KBWG_FLAG_EXACT_ORDER or 0. */
+int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                  uintptr_t n_gates, uint32_t *order, uint32_t *sweep_end, uint64_t *tile_mask,
+                  uintptr_t *n_sweeps);
+
+/* Make `device` current for this library on the calling thread; kbwg_new
+ * places new handles on the current device (0 unless selected). */
+int32_t kbwg_select_device(int32_t device);
+
+/* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
+int32_t kbwg_stream(kbwg_sim *sim, void **stream);
+
+/* Per-launch timing of the gate kernels (fused sweeps and single-gate
+ * passes) with CUDA events on the handle's stream.  enable != 0 starts a new
+ * measurement; kbwg_profile_read waits for the stream and returns the launch
+ * count, the summed device time and the summed algorithmic bytes
+ * (2 x amplitude bytes x 2^n per full pass). */
+int32_t kbwg_profile(kbwg_sim *sim, int32_t enable);
+int32_t kbwg_profile_read(kbwg_sim *sim, uint64_t *launches, double *total_ms, double *bytes);
+
+/* Bytes this library copied host->device and device->host (all handles). */
+int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h);
+
+/* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
+int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
+
+/* Text of the last error on this thread ("" if none). */
+const char *kbwg_last_error(void);
+
+/* Number of kernels this library has launched in this process (all handles). */
+uint64_t kbwg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

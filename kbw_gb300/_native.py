@@ -1,0 +1,124 @@
+"""ctypes binding of the engine's C ABI (include/kbwg.h).
+
+The library is built in-tree by ``kbw_gb300/build.py`` (or
+``__graft_entry__.build()``).  Loading fails loudly when it is missing: there
+is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkbwg.so")
+
+OK, EINVAL, EQUBITS, ENOMEM, ECUDA, EWEIGHT, ECAPACITY, ETIMEOUT, EUNSUPPORTED = range(9)
+C64, C128 = 0, 1
+FLAG_NO_FUSION = 1
+FLAG_FAST_C128 = 2
+FLAG_EXACT_ORDER = 4
+
+
+class KbwgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("kbwg error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Gate(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("target", ctypes.c_uint32),
+                ("control_mask", ctypes.c_uint64), ("angle", ctypes.c_double)]
+
+
+# name -> (restype, argtypes); every function declared in include/kbwg.h
+_P = ctypes.c_void_p
+_U = ctypes.c_size_t  # uintptr_t
+_UP = ctypes.POINTER(ctypes.c_size_t)
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    "kbwg_new": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(_P)]),
+    "kbwg_free": (_I32, [_P]),
+    "kbwg_pauli_x": (_I32, [_P, _U, _UP, _U]),
+    "kbwg_pauli_y": (_I32, [_P, _U, _UP, _U]),
+    "kbwg_pauli_z": (_I32, [_P, _U, _UP, _U]),
+    "kbwg_hadamard": (_I32, [_P, _U, _UP, _U]),
+    "kbwg_phase": (_I32, [_P, _D, _U, _UP, _U]),
+    "kbwg_rx": (_I32, [_P, _D, _U, _UP, _U]),
+    "kbwg_ry": (_I32, [_P, _D, _U, _UP, _U]),
+    "kbwg_rz": (_I32, [_P, _D, _U, _UP, _U]),
+    "kbwg_apply_gates": (_I32, [_P, ctypes.POINTER(Gate), _U]),
+    "kbwg_measure_p1": (_I32, [_P, _U, _DP]),
+    "kbwg_measure_collapse": (_I32, [_P, _U, ctypes.c_bool, _D]),
+    "kbwg_measure": (_I32, [_P, _UP, _U, _DP, _U64P]),
+    "kbwg_dump": (_I32, [_P, _UP, _U, _U64P, _DP, _DP, _U, _UP]),
+    "kbwg_sample": (_I32, [_P, _UP, _U, _U, _DP, _U64P, _U64P, _U, _UP]),
+    "kbwg_exp_value": (_I32, [_P, ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, _DP]),
+    "kbwg_clear": (_I32, [_P]),
+    "kbwg_flush": (_I32, [_P]),
+    "kbwg_get_state": (_I32, [_P, _P, _U]),
+    "kbwg_set_state": (_I32, [_P, _P, _U]),
+    "kbwg_state_info": (_I32, [_P, _UP, ctypes.POINTER(_I32), ctypes.POINTER(_P), _UP]),
+    "kbwg_swap_qubits": (_I32, [_P, _U, _U]),
+    "kbwg_build_info": (_I32, [ctypes.POINTER(ctypes.POINTER(ctypes.c_uint8)), _UP]),
+    "kbwg_plan": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_uint32),
+                         ctypes.POINTER(ctypes.c_uint32), _U64P, _UP]),
+    "kbwg_last_flush_stats": (_I32, [_P, _U64P, _U64P]),
+    "kbwg_stream": (_I32, [_P, ctypes.POINTER(_P)]),
+    "kbwg_select_device": (_I32, [_I32]),
+    "kbwg_profile": (_I32, [_P, _I32]),
+    "kbwg_profile_read": (_I32, [_P, _U64P, _DP, _DP]),
+    "kbwg_transfer_bytes": (_I32, [_U64P, _U64P]),
+    "kbwg_last_error": (ctypes.c_char_p, []),
+    "kbwg_launch_count": (ctypes.c_uint64, []),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Load libkbwg.so (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError("kbw_gb300: %s is missing; build it with "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code):
+    if code != OK:
+        msg = _lib.kbwg_last_error().decode(errors="replace") if _lib is not None else ""
+        raise KbwgError(code, msg)
+    return code
+
+
+def launch_count():
+    return int(load().kbwg_launch_count())
+
+
+def select_device(device):
+    check(load().kbwg_select_device(int(device)))
+
+
+def transfer_bytes():
+    h2d = ctypes.c_uint64()
+    d2h = ctypes.c_uint64()
+    check(load().kbwg_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h)))
+    return int(h2d.value), int(d2h.value)
+
+
+def build_info():
+    lib = load()
+    msg = ctypes.POINTER(ctypes.c_uint8)()
+    size = ctypes.c_size_t()
+    check(lib.kbwg_build_info(ctypes.byref(msg), ctypes.byref(size)))
+    return ctypes.string_at(msg, size.value).decode()

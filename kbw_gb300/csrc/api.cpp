@@ -1,0 +1,778 @@
+// extern "C" boundary of the engine (declared in include/kbwg.h).  Every
+// entry validates its arguments, turns CUDA failures into status codes and
+// never lets an exception cross the ABI.
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/kbwg.h"
+#include "sim.h"
+#include "sweep.h"
+
+namespace kbwg {
+
+std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_h2d_bytes{0}, g_d2h_bytes{0};
+static thread_local std::string g_last_error;
+
+void set_error(int32_t code, const std::string &msg) {
+    (void)code;
+    g_last_error = msg;
+}
+
+cudaError_t DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, (size_t)4096);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+}
+
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+GateDesc make_gate_desc(int prec, uint32_t kind, uint32_t target, uint64_t ctrl, double angle) {
+    GateDesc g;
+    memset(&g, 0, sizeof g);
+    g.kind = kind;
+    g.target = target;
+    g.ctrl = ctrl;
+    if (prec) {  // Dense<f64>
+        switch (kind) {
+        case G_H: g.c[0] = 0.70710678118654752440; break;
+        case G_P: g.c[0] = cos(angle); g.c[1] = sin(angle); break;
+        case G_RX:
+        case G_RY: g.c[0] = cos(angle / 2.0); g.c[1] = sin(angle / 2.0); break;
+        case G_RZ:
+            g.c[0] = cos(-angle / 2.0); g.c[1] = sin(-angle / 2.0);
+            g.c[2] = cos(angle / 2.0); g.c[3] = sin(angle / 2.0);
+            break;
+        default: break;
+        }
+    } else {  // Dense<f32>: F::from(x) rounds the f64 argument to f32 first
+        switch (kind) {
+        case G_H: g.c[0] = (double)0.70710678118654752440f; break;
+        case G_P: g.c[0] = cosf((float)angle); g.c[1] = sinf((float)angle); break;
+        case G_RX:
+        case G_RY: g.c[0] = cosf((float)(angle / 2.0)); g.c[1] = sinf((float)(angle / 2.0)); break;
+        case G_RZ:
+            g.c[0] = cosf((float)(-angle / 2.0)); g.c[1] = sinf((float)(-angle / 2.0));
+            g.c[2] = cosf((float)(angle / 2.0)); g.c[3] = sinf((float)(angle / 2.0));
+            break;
+        default: break;
+        }
+    }
+    return g;
+}
+
+double host_uniform_scale(double total) {
+    const double max_rand = 1.0 - DBL_EPSILON;
+    double scale = total;
+    while (scale * max_rand >= total) {
+        uint64_t u;
+        memcpy(&u, &scale, 8);
+        u -= 1;
+        memcpy(&scale, &u, 8);
+    }
+    return scale;
+}
+
+// splitmix64 -> 52-bit uniform in [0, 1).  Used only when the caller passes
+// no draws; it is not rand's StdRng stream.
+double next_draw(Sim &s) {
+    uint64_t z = (s.rng += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 12) * (1.0 / 4503599627370496.0);
+}
+
+template <class T>
+static cudaError_t flush_t(Sim &s) {
+    if (s.queue.empty()) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    s.last_gates = s.queue.size();
+    if (s.flags & KBWG_FLAG_NO_FUSION) {
+        for (const GateDesc &g : s.queue) {
+            if (s.prof.on) s.prof.mark(s.stream);
+            e = launch_gate1<T>(s.state, s.n, g, s.stream);
+            if (s.prof.on) {
+                s.prof.mark(s.stream);
+                s.prof.bytes += 2.0 * (double)s.elem * (double)s.ns;
+            }
+            if (e != cudaSuccess) break;
+        }
+        s.last_passes = s.queue.size();
+    } else {
+        e = run_fused(s, s.queue.data(), s.queue.size());
+    }
+    s.queue.clear();
+    return e;
+}
+
+cudaError_t flush_queue(Sim &s) { return s.prec ? flush_t<double>(s) : flush_t<float>(s); }
+
+}  // namespace kbwg
+
+using namespace kbwg;
+
+struct kbwg_sim : public Sim {};
+
+#define CUDA_TRY(expr)                                                                            \
+    do {                                                                                          \
+        cudaError_t _e = (expr);                                                                  \
+        if (_e != cudaSuccess) {                                                                  \
+            set_error(KBWG_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));            \
+            return KBWG_ECUDA;                                                                    \
+        }                                                                                         \
+    } while (0)
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                                   \
+    }                                                               \
+    catch (const std::bad_alloc &) {                                \
+        set_error(KBWG_ENOMEM, "host allocation failed");           \
+        return KBWG_ENOMEM;                                         \
+    }                                                               \
+    catch (...) {                                                   \
+        set_error(KBWG_EINVAL, "unexpected exception");             \
+        return KBWG_EINVAL;                                         \
+    }
+
+static int32_t fail(int32_t code, const char *msg) {
+    set_error(code, msg);
+    return code;
+}
+
+static int32_t select_device(kbwg_sim *s) {
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != s->device) CUDA_TRY(cudaSetDevice(s->device));
+    return KBWG_OK;
+}
+
+#define ENTER(sim)                                            \
+    if (!(sim)) return fail(KBWG_EINVAL, "null handle");      \
+    {                                                         \
+        int32_t _r = select_device(sim);                      \
+        if (_r) return _r;                                    \
+    }
+
+template <class F>
+static auto dispatch(kbwg_sim *s, F &&f) -> decltype(f((float *)nullptr)) {
+    return s->prec ? f((double *)nullptr) : f((float *)nullptr);
+}
+
+extern "C" {
+
+int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_sim **out) {
+    GUARD_BEGIN
+    if (!out) return fail(KBWG_EINVAL, "null out pointer");
+    *out = nullptr;
+    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32 (Dense limit)");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    kbwg_sim *s = new kbwg_sim();
+    s->n = (uint32_t)num_qubits;
+    s->prec = precision;
+    s->flags = flags;
+    s->ns = 1ull << num_qubits;
+    s->elem = precision ? 16 : 8;
+    CUDA_TRY(cudaGetDevice(&s->device));
+    auto cleanup = [&](int32_t code, const std::string &m) {
+        kbwg_free(s);
+        set_error(code, m);
+        return code;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
+    e = cudaMalloc(&s->state, s->ns * s->elem);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(KBWG_ENOMEM, std::string("state allocation: ") + cudaGetErrorString(e));
+    }
+    const size_t part = (size_t)kReduceBlocks * kMaxTerms * sizeof(double);
+    const size_t scratch_bytes = part + 256 + 256 + sizeof(MeasureCtl) + 256;
+    e = cudaMalloc(&s->scratch, scratch_bytes);
+    if (e != cudaSuccess) return cleanup(KBWG_ENOMEM, "scratch allocation");
+    char *p = (char *)s->scratch;
+    s->rs.partials = (double *)p;
+    s->rs.ticket = (unsigned *)(p + part);
+    s->rs.result = (double *)(p + part + 256);
+    s->d_ctl = (MeasureCtl *)(p + part + 512);
+    s->d_err = (int *)(p + part + 128);
+    e = cudaMemsetAsync(s->scratch, 0, scratch_bytes, s->stream);
+    if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
+    e = cudaMallocHost(&s->h_ctl, sizeof(MeasureCtl) + kMaxTerms * sizeof(double));
+    if (e != cudaSuccess) return cleanup(KBWG_ENOMEM, "pinned allocation");
+    s->h_result = (double *)(s->h_ctl + 1);
+    const char *seed = getenv("KBW_SEED");
+    char *end = nullptr;
+    unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
+    s->rng = (seed && end && *end == 0 && *seed) ? (uint64_t)sv : (uint64_t)(uintptr_t)s ^ 0x5DEECE66Dull;
+    e = s->prec ? launch_init<double>(s->state, s->n, s->stream) : launch_init<float>(s->state, s->n, s->stream);
+    if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
+    *out = s;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_free(kbwg_sim *s) {
+    GUARD_BEGIN
+    if (!s) return KBWG_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->state) cudaFree(s->state);
+    if (s->scratch) cudaFree(s->scratch);
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
+    s->tmp0.release();
+    s->tmp1.release();
+    s->tmp2.release();
+    s->tmp3.release();
+    s->tmp4.release();
+    s->tmp5.release();
+    s->prof.release();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return KBWG_OK;
+    GUARD_END
+}
+
+static int32_t push_gate(kbwg_sim *s, uint32_t kind, double angle, uintptr_t target, const uintptr_t *control,
+                         uintptr_t n_control) {
+    GUARD_BEGIN
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
+    if (n_control && !control) return fail(KBWG_EINVAL, "null control list");
+    uint64_t mask = 0;
+    for (uintptr_t i = 0; i < n_control; i++) {
+        if (control[i] >= s->n) return fail(KBWG_EINVAL, "control qubit out of range");
+        if (control[i] == target) return fail(KBWG_EINVAL, "control equals target");
+        mask |= 1ull << control[i];
+    }
+    s->queue.push_back(make_gate_desc(s->prec, kind, (uint32_t)target, mask, angle));
+    if (s->queue.size() >= 65536) {
+        ENTER(s);
+        CUDA_TRY(flush_queue(*s));
+    }
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_pauli_x(kbwg_sim *s, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_X, 0.0, t, c, nc); }
+int32_t kbwg_pauli_y(kbwg_sim *s, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_Y, 0.0, t, c, nc); }
+int32_t kbwg_pauli_z(kbwg_sim *s, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_Z, 0.0, t, c, nc); }
+int32_t kbwg_hadamard(kbwg_sim *s, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_H, 0.0, t, c, nc); }
+int32_t kbwg_phase(kbwg_sim *s, double a, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_P, a, t, c, nc); }
+int32_t kbwg_rx(kbwg_sim *s, double a, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_RX, a, t, c, nc); }
+int32_t kbwg_ry(kbwg_sim *s, double a, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_RY, a, t, c, nc); }
+int32_t kbwg_rz(kbwg_sim *s, double a, uintptr_t t, const uintptr_t *c, uintptr_t nc) { return push_gate(s, G_RZ, a, t, c, nc); }
+
+int32_t kbwg_apply_gates(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates) {
+    GUARD_BEGIN
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    if (n_gates && !gates) return fail(KBWG_EINVAL, "null gate list");
+    const uint64_t all = (s->n >= 64) ? ~0ull : ((1ull << s->n) - 1);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ) return fail(KBWG_EINVAL, "bad gate kind");
+        if (g.target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
+        if (g.control_mask & ~all) return fail(KBWG_EINVAL, "control qubit out of range");
+        if (g.control_mask & (1ull << g.target)) return fail(KBWG_EINVAL, "control equals target");
+    }
+    s->queue.reserve(s->queue.size() + n_gates);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        s->queue.push_back(make_gate_desc(s->prec, g.kind, g.target, g.control_mask, g.angle));
+    }
+    if (s->queue.size() >= 65536) {
+        ENTER(s);
+        CUDA_TRY(flush_queue(*s));
+    }
+    return KBWG_OK;
+    GUARD_END
+}
+
+static int32_t check_device_error(kbwg_sim *s) {
+    int flag = 0;
+    CUDA_TRY(copy_async(&flag, s->d_err, sizeof flag, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (flag) {
+        CUDA_TRY(cudaMemsetAsync(s->d_err, 0, sizeof flag, s->stream));
+        return fail(KBWG_ETIMEOUT, "a device-side bounded wait ran out; the state is not valid");
+    }
+    return KBWG_OK;
+}
+
+int32_t kbwg_flush(kbwg_sim *s) {
+    GUARD_BEGIN
+    ENTER(s);
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return check_device_error(s);
+    GUARD_END
+}
+
+int32_t kbwg_measure_p1(kbwg_sim *s, uintptr_t target, double *p1) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!p1) return fail(KBWG_EINVAL, "null output");
+    if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
+    CUDA_TRY(flush_queue(*s));
+    const uint64_t bit = 1ull << target;
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_masked_norm<T>(s->state, s->n, bit, bit, s->rs, s->stream);
+    }));
+    CUDA_TRY(copy_async(s->h_result, s->rs.result, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *p1 = s->h_result[0];
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_measure_collapse(kbwg_sim *s, uintptr_t target, bool result, double p) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
+    CUDA_TRY(flush_queue(*s));
+    const uint64_t bit = 1ull << target;
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_collapse<T>(s->state, s->n, nullptr, bit, result ? bit : 0ull, p, s->stream);
+    }));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_measure(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, const double *draws,
+                     uint64_t *result) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!result || (n_qubits && !qubits)) return fail(KBWG_EINVAL, "null argument");
+    if (n_qubits > 64) return fail(KBWG_EINVAL, "more than 64 qubits in one measurement");
+    uint64_t seen = 0;
+    for (uintptr_t i = 0; i < n_qubits; i++) {
+        if (qubits[i] >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+        if (seen & (1ull << qubits[i])) return fail(KBWG_EINVAL, "qubit listed twice");
+        seen |= 1ull << qubits[i];
+    }
+    *result = 0;
+    if (n_qubits == 0) return KBWG_OK;
+    CUDA_TRY(flush_queue(*s));
+    MeasureCtl &c = *s->h_ctl;
+    memset(&c, 0, sizeof c);
+    c.scale2 = 1.0;
+    for (uintptr_t k = 0; k < n_qubits; k++) {
+        c.qubit[k] = (uint32_t)qubits[n_qubits - 1 - k];  // last listed first
+        c.draws[k] = draws ? draws[k] : next_draw(*s);
+    }
+    CUDA_TRY(copy_async(s->d_ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        for (uint32_t k = 0; k < n_qubits; k++) {
+            cudaError_t e = launch_measure_step<T>(s->state, s->n, s->d_ctl, k, s->rs, s->stream);
+            if (e != cudaSuccess) return e;
+        }
+        return launch_collapse<T>(s->state, s->n, s->d_ctl, 0, 0, 0.0, s->stream);
+    }));
+    CUDA_TRY(copy_async(&c, s->d_ctl, sizeof c, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *result = c.result;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_dump(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, uint64_t *basis_states, double *re,
+                  double *im, uintptr_t capacity, uintptr_t *size) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!size || (n_qubits && !qubits)) return fail(KBWG_EINVAL, "null argument");
+    if (n_qubits > 64) return fail(KBWG_EINVAL, "more than 64 qubits");
+    for (uintptr_t i = 0; i < n_qubits; i++)
+        if (qubits[i] >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+    CUDA_TRY(flush_queue(*s));
+    const int B = dump_blocks(s->n);
+    CUDA_TRY(s->tmp0.ensure((size_t)B * 8));
+    uint64_t *d_counts = (uint64_t *)s->tmp0.ptr;
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_dump_count<T>(s->state, s->n, d_counts, s->stream);
+    }));
+    std::vector<uint64_t> counts(B), offs(B + 1);
+    CUDA_TRY(copy_async(counts.data(), d_counts, (size_t)B * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    offs[0] = 0;
+    for (int b = 0; b < B; b++) offs[b + 1] = offs[b] + counts[b];
+    const uint64_t total = offs[B];
+    *size = (uintptr_t)total;
+    if (capacity < total) {
+        if (capacity == 0 && !basis_states) return KBWG_OK;  // size query
+        set_error(KBWG_ECAPACITY, "dump capacity too small");
+        return KBWG_ECAPACITY;
+    }
+    if (!basis_states || !re || !im) return fail(KBWG_EINVAL, "null output buffer");
+    if (total == 0) return KBWG_OK;
+    DumpSpec spec;
+    memset(&spec, 0, sizeof spec);
+    spec.nq = (uint32_t)n_qubits;
+    for (uintptr_t i = 0; i < n_qubits; i++) spec.qubits[i] = (uint8_t)qubits[i];
+    CUDA_TRY(s->tmp1.ensure((size_t)(B + 1) * 8));
+    CUDA_TRY(s->tmp2.ensure((size_t)total * 24));
+    uint64_t *d_off = (uint64_t *)s->tmp1.ptr;
+    uint64_t *d_states = (uint64_t *)s->tmp2.ptr;
+    double *d_re = (double *)(d_states + total);
+    double *d_im = d_re + total;
+    CUDA_TRY(copy_async(d_off, offs.data(), (size_t)(B + 1) * 8, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_dump_write<T>(s->state, s->n, d_off, spec, d_states, d_re, d_im, s->stream);
+    }));
+    CUDA_TRY(copy_async(basis_states, d_states, total * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(copy_async(re, d_re, total * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(copy_async(im, d_im, total * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_sample(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, uintptr_t shots, const double *draws,
+                    uint64_t *states, uint64_t *counts, uintptr_t capacity, uintptr_t *n_out) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!n_out || (n_qubits && !qubits) || (shots && (!states || !counts)))
+        return fail(KBWG_EINVAL, "null argument");
+    if (n_qubits > 64) return fail(KBWG_EINVAL, "more than 64 qubits");
+    for (uintptr_t i = 0; i < n_qubits; i++)
+        if (qubits[i] >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+    *n_out = 0;
+    const uint64_t need = std::min<uint64_t>(shots, n_qubits >= 64 ? ~0ull : (1ull << n_qubits));
+    if (capacity < need) {
+        set_error(KBWG_ECAPACITY, "sample capacity too small");
+        return KBWG_ECAPACITY;
+    }
+    CUDA_TRY(flush_queue(*s));
+    const int B = sample_blocks(s->n);
+    CUDA_TRY(s->tmp0.ensure((size_t)B * 8));
+    double *d_bs = (double *)s->tmp0.ptr;
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_weight_blocksum<T>(s->state, s->n, d_bs, s->stream);
+    }));
+    std::vector<double> bs(B), pre(B + 1);
+    CUDA_TRY(copy_async(bs.data(), d_bs, (size_t)B * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    pre[0] = 0.0;
+    for (int b = 0; b < B; b++) pre[b + 1] = pre[b] + bs[b];
+    const double total = pre[B];
+    if (!(total > 0.0)) return fail(KBWG_EWEIGHT, "all sampling weights are zero");
+    if (shots == 0) return KBWG_OK;
+    const double scale = host_uniform_scale(total);
+    std::vector<double> chosen(shots);
+    for (uintptr_t k = 0; k < shots; k++) chosen[k] = (draws ? draws[k] : next_draw(*s)) * scale;
+    std::sort(chosen.begin(), chosen.end());
+    // block of each shot: first b whose end prefix exceeds the chosen weight
+    std::vector<uint32_t> blocks;
+    std::vector<uint64_t> begin;
+    std::vector<double> bprefix;
+    int b = 0;
+    for (uintptr_t k = 0; k < shots; k++) {
+        while (b < B - 1 && !(pre[b + 1] > chosen[k])) b++;
+        if (blocks.empty() || blocks.back() != (uint32_t)b) {
+            blocks.push_back((uint32_t)b);
+            begin.push_back(k);
+            bprefix.push_back(pre[b]);
+        }
+    }
+    begin.push_back(shots);
+    const size_t nb = blocks.size();
+    const size_t bytes = nb * 4 + (nb + 1) * 8 + nb * 8 + shots * 8 + shots * 8 + 64;
+    CUDA_TRY(s->tmp1.ensure(bytes));
+    char *base = (char *)s->tmp1.ptr;
+    uint64_t *d_pick = (uint64_t *)base;
+    double *d_chosen = (double *)(d_pick + shots);
+    uint64_t *d_begin = (uint64_t *)(d_chosen + shots);
+    double *d_pre = (double *)(d_begin + nb + 1);
+    uint32_t *d_blocks = (uint32_t *)(d_pre + nb);
+    CUDA_TRY(copy_async(d_chosen, chosen.data(), shots * 8, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(copy_async(d_begin, begin.data(), (nb + 1) * 8, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(copy_async(d_pre, bprefix.data(), nb * 8, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(copy_async(d_blocks, blocks.data(), nb * 4, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_sample_pick<T>(s->state, s->n, d_blocks, (uint32_t)nb, d_begin, d_pre, d_chosen, d_pick,
+                                     s->stream);
+    }));
+    std::vector<uint64_t> pick(shots);
+    CUDA_TRY(copy_async(pick.data(), d_pick, shots * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (uintptr_t k = 0; k < shots; k++) {
+        uint64_t packed = 0;
+        for (uintptr_t j = 0; j < n_qubits; j++) packed |= ((pick[k] >> qubits[n_qubits - 1 - j]) & 1ull) << j;
+        pick[k] = packed;
+    }
+    std::sort(pick.begin(), pick.end());
+    uintptr_t m = 0;
+    for (uintptr_t k = 0; k < shots; k++) {
+        if (m > 0 && states[m - 1] == pick[k]) {
+            counts[m - 1]++;
+        } else {
+            states[m] = pick[k];
+            counts[m] = 1;
+            m++;
+        }
+    }
+    *n_out = m;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubits, const uintptr_t *offsets,
+                       const double *coefficients, uintptr_t n_strings, double *out) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!out || (n_strings && (!offsets || !coefficients))) return fail(KBWG_EINVAL, "null argument");
+    struct Str {
+        uint64_t x, z;
+        int ny;
+    };
+    std::vector<Str> strs(n_strings);
+    for (uintptr_t k = 0; k < n_strings; k++) {
+        Str t{0, 0, 0};
+        if (offsets[k + 1] < offsets[k]) return fail(KBWG_EINVAL, "offsets not ascending");
+        for (uintptr_t i = offsets[k]; i < offsets[k + 1]; i++) {
+            if (!paulis || !qubits) return fail(KBWG_EINVAL, "null term arrays");
+            const uintptr_t q = qubits[i];
+            if (q >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+            const uint64_t bit = 1ull << q;
+            if ((t.x | t.z) & bit) return fail(KBWG_EINVAL, "qubit repeated in one Pauli string");
+            switch (paulis[i]) {
+            case KBWG_PAULI_X: t.x |= bit; break;
+            case KBWG_PAULI_Y: t.x |= bit; t.z |= bit; t.ny++; break;
+            case KBWG_PAULI_Z: t.z |= bit; break;
+            default: return fail(KBWG_EINVAL, "bad Pauli code");
+            }
+        }
+        strs[k] = t;
+    }
+    CUDA_TRY(flush_queue(*s));
+    // group strings by flip mask; per group launch in chunks of kMaxTerms
+    std::vector<uintptr_t> order(n_strings);
+    for (uintptr_t k = 0; k < n_strings; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](uintptr_t a, uintptr_t b) { return strs[a].x < strs[b].x; });
+    CUDA_TRY(s->tmp3.ensure((n_strings + 1) * 8));
+    double *d_vals = (double *)s->tmp3.ptr;
+    size_t i = 0;
+    while (i < n_strings) {
+        PauliGroup g;
+        memset(&g, 0, sizeof g);
+        g.x = strs[order[i]].x;
+        std::vector<uintptr_t> idx;
+        while (i < n_strings && strs[order[i]].x == g.x && idx.size() < (size_t)kMaxTerms) {
+            const Str &t = strs[order[i]];
+            const int k = (int)idx.size();
+            g.z[k] = t.z;
+            if (g.x == 0) {
+                g.factor[k] = 1.0;
+                g.use_im[k] = 0;
+            } else {
+                const int m = t.ny & 3;
+                g.use_im[k] = (m & 1) ? 1 : 0;
+                g.factor[k] = (m == 0 || m == 1) ? 2.0 : -2.0;
+            }
+            idx.push_back(order[i]);
+            i++;
+        }
+        g.nterms = (uint32_t)idx.size();
+        CUDA_TRY(dispatch(s, [&](auto *tp) {
+            using T = std::remove_pointer_t<decltype(tp)>;
+            return launch_pauli_group<T>(s->state, s->n, g, s->rs, s->stream);
+        }));
+        for (size_t k = 0; k < idx.size(); k++)
+            CUDA_TRY(copy_async(d_vals + idx[k], s->rs.result + k, 8, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    std::vector<double> vals(n_strings + 1);
+    if (n_strings)
+        CUDA_TRY(copy_async(vals.data(), d_vals, n_strings * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double total = 0.0;  // sum in string order, as the reference's zip/map/sum
+    for (uintptr_t k = 0; k < n_strings; k++) total += vals[k] * coefficients[k];
+    *out = total;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_clear(kbwg_sim *s) {
+    GUARD_BEGIN
+    ENTER(s);
+    s->queue.clear();
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_init<T>(s->state, s->n, s->stream);
+    }));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_get_state(kbwg_sim *s, void *host_dst, uintptr_t bytes) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!host_dst || bytes != s->ns * s->elem) return fail(KBWG_EINVAL, "buffer size must equal 2^n * element size");
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(copy_async(host_dst, s->state, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return check_device_error(s);
+    GUARD_END
+}
+
+int32_t kbwg_set_state(kbwg_sim *s, const void *host_src, uintptr_t bytes) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!host_src || bytes != s->ns * s->elem) return fail(KBWG_EINVAL, "buffer size must equal 2^n * element size");
+    s->queue.clear();
+    CUDA_TRY(copy_async(s->state, host_src, bytes, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_state_info(kbwg_sim *s, uintptr_t *num_qubits, int32_t *precision, void **device_ptr,
+                        uintptr_t *bytes) {
+    GUARD_BEGIN
+    ENTER(s);
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (num_qubits) *num_qubits = s->n;
+    if (precision) *precision = s->prec;
+    if (device_ptr) *device_ptr = s->state;
+    if (bytes) *bytes = s->ns * s->elem;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_swap_qubits(kbwg_sim *s, uintptr_t a, uintptr_t b) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (a >= s->n || b >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(dispatch(s, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_swap<T>(s->state, s->n, (uint32_t)a, (uint32_t)b, s->stream);
+    }));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_build_info(const uint8_t **msg, uintptr_t *size) {
+    static const char info[] = "kbw-gb300 densegb300 v0.1 [nvcc sm_103a]";
+    if (!msg || !size) return KBWG_EINVAL;
+    *msg = (const uint8_t *)info;
+    *size = sizeof(info) - 1;
+    return KBWG_OK;
+}
+
+int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                  uintptr_t n_gates, uint32_t *order, uint32_t *sweep_end, uint64_t *tile_mask,
+                  uintptr_t *n_sweeps) {
+    GUARD_BEGIN
+    if (!n_sweeps || (n_gates && (!gates || !order || !sweep_end || !tile_mask)))
+        return fail(KBWG_EINVAL, "null argument");
+    const int K = precision ? TileCfg<double>::K : TileCfg<float>::K;
+    const int R = precision ? TileCfg<double>::R : TileCfg<float>::R;
+    if (num_qubits < (uintptr_t)K || num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits outside [K, 32]");
+    std::vector<GateDesc> gd(n_gates);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ || g.target >= num_qubits || (g.control_mask >> num_qubits) ||
+            (g.control_mask & (1ull << g.target)))
+            return fail(KBWG_EINVAL, "bad gate");
+        gd[i] = make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle);
+    }
+    std::vector<PlannedSweep> plan = plan_sweeps((uint32_t)num_qubits, K, R, gd.data(), gd.size(),
+                                                 (flags & KBWG_FLAG_EXACT_ORDER) != 0);
+    uintptr_t pos = 0;
+    for (size_t k = 0; k < plan.size(); k++) {
+        for (uint32_t i : plan[k].src) order[pos++] = i;
+        sweep_end[k] = (uint32_t)pos;
+        tile_mask[k] = ((1ull << plan[k].l) - 1) | plan[k].hmask;
+    }
+    *n_sweeps = plan.size();
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_select_device(int32_t device) {
+    CUDA_TRY(cudaSetDevice(device));
+    return KBWG_OK;
+}
+
+int32_t kbwg_stream(kbwg_sim *s, void **stream) {
+    if (!s || !stream) return fail(KBWG_EINVAL, "null argument");
+    *stream = (void *)s->stream;
+    return KBWG_OK;
+}
+
+int32_t kbwg_profile(kbwg_sim *s, int32_t enable) {
+    GUARD_BEGIN
+    ENTER(s);
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->prof.on = enable != 0;
+    s->prof.used = 0;
+    s->prof.bytes = 0.0;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_profile_read(kbwg_sim *s, uint64_t *launches, double *total_ms, double *bytes) {
+    GUARD_BEGIN
+    ENTER(s);
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double t = 0.0;
+    for (size_t i = 0; i + 1 < s->prof.used; i += 2) {
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, s->prof.pool[i], s->prof.pool[i + 1]));
+        t += ms;
+    }
+    if (launches) *launches = s->prof.used / 2;
+    if (total_ms) *total_ms = t;
+    if (bytes) *bytes = s->prof.bytes;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h) {
+    if (h2d) *h2d = g_h2d_bytes.load();
+    if (d2h) *d2h = g_d2h_bytes.load();
+    return KBWG_OK;
+}
+
+int32_t kbwg_last_flush_stats(kbwg_sim *s, uint64_t *gates, uint64_t *passes) {
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    if (gates) *gates = s->last_gates;
+    if (passes) *passes = s->last_passes;
+    return KBWG_OK;
+}
+
+const char *kbwg_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t kbwg_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

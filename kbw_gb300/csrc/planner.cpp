@@ -1,0 +1,169 @@
+// Host fusion planner for the tile sweeps (pure C++, no CUDA calls).
+#include <string.h>
+
+#include <algorithm>
+
+#include "sweep.h"
+
+namespace kbwg {
+
+bool is_diagonal(uint32_t kind) { return kind == G_Z || kind == G_P || kind == G_RZ; }
+
+static inline uint64_t qubits_of(const GateDesc &g) { return g.ctrl | (1ull << g.target); }
+
+// Choose the tile's contiguous low block l (as large as possible) and its
+// high qubits: every needed high target, padded up to K qubits.
+static void choose_tile(uint32_t n, int K, uint64_t needed, PlannedSweep &sw) {
+    int l = K;
+    for (; l >= kLaneBits; l--) {
+        const uint64_t above = (l >= 64) ? 0 : (needed & ~((1ull << l) - 1));
+        if (l + __builtin_popcountll(above) <= K) break;
+    }
+    uint64_t h = needed & ~((1ull << l) - 1);
+    for (uint32_t q = l; q < n && l + __builtin_popcountll(h) < K; q++) h |= 1ull << q;
+    sw.l = (uint32_t)l;
+    sw.hmask = h;
+    sw.m = 0;
+    for (uint32_t q = 0; q < 64; q++)
+        if (h >> q & 1) sw.hq[sw.m++] = (uint8_t)q;
+}
+
+static inline int local_bit(const PlannedSweep &sw, uint32_t q) {
+    if (q < sw.l) return (int)q;
+    for (uint32_t j = 0; j < sw.m; j++)
+        if (sw.hq[j] == q) return (int)(sw.l + j);
+    return -1;
+}
+
+static inline bool runs_in(int lb, int layout, int K, int R) {
+    if (lb < kLaneBits) return true;
+    if (layout == LAYOUT_A) return lb < kLaneBits + R;
+    return lb >= K - R;
+}
+
+std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *g, size_t count,
+                                      bool keep_order) {
+    std::vector<PlannedSweep> out;
+    std::vector<size_t> remaining(count);
+    for (size_t i = 0; i < count; i++) remaining[i] = i;
+    const size_t window = 8192;  // gates examined per sweep
+    while (!remaining.empty()) {
+        // 1. choose the sweep's gates
+        uint64_t needed = 0, blocked = 0;
+        const int max_high = K - kLaneBits;
+        std::vector<size_t> take, rest;
+        const size_t scan = std::min(remaining.size(), window);
+        for (size_t ii = 0; ii < scan; ii++) {
+            const size_t i = remaining[ii];
+            const GateDesc &x = g[i];
+            const uint64_t qs = qubits_of(x);
+            bool ok = !(qs & blocked);
+            if (ok && !is_diagonal(x.kind) && x.target >= (uint32_t)kLaneBits) {
+                const uint64_t b = 1ull << x.target;
+                if (!(needed & b)) {
+                    if (__builtin_popcountll(needed) < max_high)
+                        needed |= b;
+                    else
+                        ok = false;
+                }
+            }
+            if (ok) {
+                take.push_back(i);
+            } else {
+                rest.push_back(i);
+                blocked |= qs;
+                if (keep_order) blocked = ~0ull;  // nothing may pass a deferred gate
+            }
+        }
+        for (size_t ii = scan; ii < remaining.size(); ii++) rest.push_back(remaining[ii]);
+
+        PlannedSweep sw;
+        choose_tile(n, K, needed, sw);
+        const uint64_t tile_mask = ((1ull << sw.l) - 1) | sw.hmask;
+
+        // 2. order the taken gates into register-layout stages
+        std::vector<size_t> pending = take, leftover;
+        int layout = LAYOUT_A;
+        // start in the layout the first register-bound gate wants
+        for (size_t i : pending) {
+            const GateDesc &x = g[i];
+            if (is_diagonal(x.kind)) continue;
+            const int lb = local_bit(sw, x.target);
+            if (lb >= kLaneBits) {
+                layout = runs_in(lb, LAYOUT_A, K, R) ? LAYOUT_A : LAYOUT_B;
+                break;
+            }
+        }
+        int idle_switches = 0;
+        while (!pending.empty()) {
+            if ((int)sw.stage_layout.size() == kMaxStages) {
+                leftover = pending;
+                break;
+            }
+            std::vector<size_t> now, later;
+            uint64_t blk = 0;
+            for (size_t i : pending) {
+                const GateDesc &x = g[i];
+                const uint64_t qs = qubits_of(x);
+                bool ok = !(qs & blk);
+                if (ok && !is_diagonal(x.kind)) ok = runs_in(local_bit(sw, x.target), layout, K, R);
+                if (ok) {
+                    now.push_back(i);
+                } else {
+                    later.push_back(i);
+                    blk |= qs;
+                    if (keep_order) blk = ~0ull;
+                }
+            }
+            if (now.empty()) {
+                if (++idle_switches > 2) {  // cannot happen for a valid tile; guard anyway
+                    leftover = pending;
+                    break;
+                }
+                layout ^= 1;
+                continue;
+            }
+            idle_switches = 0;
+            for (size_t i : now) {
+                const GateDesc &x = g[i];
+                TileGate t;
+                memset(&t, 0, sizeof t);
+                t.kind = x.kind;
+                memcpy(t.c, x.c, sizeof t.c);
+                const int lb = local_bit(sw, x.target);
+                if (lb < 0) {  // diagonal gate on a qubit outside the tile
+                    t.flags = TG_OUTER_TARGET;
+                    t.tout = 1ull << x.target;
+                } else {
+                    t.tb = (uint32_t)lb;
+                }
+                uint64_t cm = x.ctrl;
+                while (cm) {
+                    const uint32_t q = __builtin_ctzll(cm);
+                    cm &= cm - 1;
+                    const int cb = (tile_mask >> q & 1) ? local_bit(sw, q) : -1;
+                    if (cb >= 0)
+                        t.cl |= 1u << cb;
+                    else
+                        t.co |= 1ull << q;
+                }
+                sw.gates.push_back(t);
+                sw.src.push_back((uint32_t)i);
+            }
+            sw.stage_layout.push_back((uint8_t)layout);
+            sw.stage_end.push_back((uint16_t)sw.gates.size());
+            pending.swap(later);
+            layout ^= 1;
+        }
+        // gates that did not fit go back in front, in program order
+        std::sort(leftover.begin(), leftover.end());
+        std::vector<size_t> next;
+        next.reserve(leftover.size() + rest.size());
+        std::merge(leftover.begin(), leftover.end(), rest.begin(), rest.end(), std::back_inserter(next));
+        remaining.swap(next);
+        if (!sw.gates.empty()) out.push_back(std::move(sw));
+    }
+    return out;
+}
+
+}  // namespace kbwg

@@ -1,0 +1,593 @@
+// Reductions over the state: probabilities, sequential measurement,
+// collapse, Pauli-string expectation values, dump compaction and sampling.
+//
+// Every reduction runs on a fixed grid and finishes in the last block to
+// arrive (ticket counter, no spin-wait), so results are deterministic run to
+// run.  Accumulation is FP64-grade: native double for complex128 data and
+// float-float (error-free products and sums) for complex64 data, widened to
+// double per thread before the block tree.
+#include <float.h>
+
+#include "kernels.h"
+
+namespace kbwg {
+
+// ---- accumulators ---------------------------------------------------------
+struct AccF {  // float-float running sum of products
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add2(float p, float e) {
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        err = __fadd_rn(err, __fadd_rn(lo, e));
+        hi = __fadd_rn(s, err);
+        lo = __fsub_rn(err, __fsub_rn(hi, s));
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        add2(p, __fmaf_rn(a, b, -p));
+    }
+    __device__ __forceinline__ void add_prod_neg(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        add2(-p, -__fmaf_rn(a, b, -p));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+struct AccD {
+    double v = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { v = __fma_rn(a, b, v); }
+    __device__ __forceinline__ void add_prod_neg(double a, double b) { v = __fma_rn(-a, b, v); }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <class T> struct AccOf;
+template <> struct AccOf<float> { using type = AccF; };
+template <> struct AccOf<double> { using type = AccD; };
+
+// float-float value (products kept exactly)
+struct FF {
+    float hi, lo;
+};
+
+// ---- block helpers ----------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block; the result is valid in thread 0.
+__device__ double block_sum(double v) {
+    __shared__ double sh[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// Inclusive scan over the block in a fixed order; also returns the total.
+__device__ double block_inclusive_scan(double v, double *total) {
+    __shared__ double wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    __syncthreads();
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        double x = (lane < nw) ? wsum[lane] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < nw) wsum[lane] = x;  // inclusive warp prefix
+    }
+    __syncthreads();
+    if (w > 0) v += wsum[w - 1];
+    *total = wsum[(blockDim.x >> 5) - 1];
+    return v;
+}
+
+// True in the last block to finish; partials written before are visible.
+__device__ bool last_block(unsigned *ticket) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    return is_last;
+}
+
+// Deterministic sum of partials[b * stride + k] over b by the whole block.
+__device__ double sum_partials(const double *partials, int nblocks, int stride, int k) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += partials[(size_t)b * stride + k];
+    return block_sum(v);
+}
+
+__device__ __forceinline__ uint64_t insert_zero(uint64_t i, uint32_t m) {
+    const uint64_t low = (1ull << m) - 1;
+    return ((i & ~low) << 1) | (i & low);
+}
+
+// Insert zero bits at every set position of M (ascending).
+__device__ __forceinline__ uint64_t insert_zeros(uint64_t i, uint64_t M) {
+    while (M) {
+        const uint32_t m = __ffsll((long long)M) - 1;
+        M &= M - 1;
+        i = insert_zero(i, m);
+    }
+    return i;
+}
+
+// rand's UniformFloat::new(0, total) scale rule (largest draw 1 - 2^-52).
+__host__ __device__ inline double uniform_scale(double total) {
+    const double max_rand = 1.0 - DBL_EPSILON;
+    double scale = total;
+#ifdef __CUDA_ARCH__
+    while (__dmul_rn(scale, max_rand) >= total) scale = __longlong_as_double(__double_as_longlong(scale) - 1);
+#else
+    while (scale * max_rand >= total) {
+        union {
+            double d;
+            uint64_t u;
+        } x;
+        x.d = scale;
+        x.u -= 1;
+        scale = x.d;
+    }
+#endif
+    return scale;
+}
+
+// ---- masked norm / p1 -------------------------------------------------------
+template <class T>
+__device__ __forceinline__ double masked_norm_body(const cx<T> *__restrict__ st, uint64_t count, uint64_t M,
+                                                   uint64_t V) {
+    typename AccOf<T>::type acc;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < count; i += 4 * stride) {
+        cx<T> a[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[u] = st[insert_zeros(i + u * stride, M) | V];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            acc.add_prod(a[u].re, a[u].re);
+            acc.add_prod(a[u].im, a[u].im);
+        }
+    }
+    for (; i < count; i += stride) {
+        const cx<T> a = st[insert_zeros(i, M) | V];
+        acc.add_prod(a.re, a.re);
+        acc.add_prod(a.im, a.im);
+    }
+    return block_sum(acc.value());
+}
+
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads)
+    k_masked_norm(const cx<T> *__restrict__ st, uint64_t count, uint64_t M, uint64_t V, ReduceScratch rs) {
+    const double v = masked_norm_body<T>(st, count, M, V);
+    if (threadIdx.x == 0) rs.partials[blockIdx.x] = v;
+    if (last_block(rs.ticket)) {
+        const double t = sum_partials(rs.partials, gridDim.x, 1, 0);
+        if (threadIdx.x == 0) {
+            rs.result[0] = t;
+            *rs.ticket = 0;
+        }
+    }
+}
+
+template <class T>
+cudaError_t launch_masked_norm(const void *st, uint32_t n, uint64_t M, uint64_t V, const ReduceScratch &rs,
+                               cudaStream_t s) {
+    const uint64_t count = 1ull << (n - __builtin_popcountll(M));
+    k_masked_norm<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, count, M, V, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---- sequential measurement step ------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads)
+    k_measure_step(const cx<T> *__restrict__ st, uint32_t n, MeasureCtl *ctl, uint32_t step, ReduceScratch rs) {
+    const uint64_t bit = 1ull << ctl->qubit[step];
+    const uint64_t M = ctl->M | bit, V = ctl->V | bit;
+    const uint64_t count = 1ull << (n - __popcll(M));
+    const double v = masked_norm_body<T>(st, count, M, V);
+    if (threadIdx.x == 0) rs.partials[blockIdx.x] = v;
+    if (last_block(rs.ticket)) {
+        const double s1 = sum_partials(rs.partials, gridDim.x, 1, 0);
+        if (threadIdx.x == 0) {
+            // QubitManager::do_measure decision (src/quantum_execution.rs:278-287)
+            const double p1 = __dmul_rn(s1, ctl->scale2);
+            double p0 = __dsub_rn(1.0, p1);
+            if (!(p0 > 0.0)) p0 = 0.0;
+            const double total = __dadd_rn(p0, p1);
+            const double chosen = __dmul_rn(ctl->draws[step], uniform_scale(total));
+            const int r = (p0 <= chosen) ? 1 : 0;
+            double prob = r ? p1 : p0;
+            if (!(prob > DBL_MIN)) prob = DBL_MIN;
+            const double p = 1.0 / sqrt(prob);
+            const double pf = (double)(T)p;
+            ctl->p[step] = p;
+            ctl->scale2 = __dmul_rn(__dmul_rn(ctl->scale2, pf), pf);
+            ctl->M = ctl->M | bit;
+            ctl->V = ctl->V | (r ? bit : 0ull);
+            ctl->result |= (uint64_t)r << step;
+            ctl->steps = step + 1;
+            *rs.ticket = 0;
+        }
+    }
+}
+
+template <class T>
+cudaError_t launch_measure_step(const void *st, uint32_t n, MeasureCtl *ctl, uint32_t step,
+                                const ReduceScratch &rs, cudaStream_t s) {
+    k_measure_step<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, n, ctl, step, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---- collapse -----------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256)
+    k_collapse(cx<T> *__restrict__ st, uint64_t ns, const MeasureCtl *ctl, uint64_t M, uint64_t V, double p) {
+    __shared__ T pf[64];
+    __shared__ uint64_t sM, sV;
+    __shared__ uint32_t nf;
+    if (threadIdx.x == 0) {
+        if (ctl) {
+            sM = ctl->M;
+            sV = ctl->V;
+            nf = ctl->steps;
+        } else {
+            sM = M;
+            sV = V;
+            nf = 1;
+        }
+    }
+    if (threadIdx.x < 64) pf[threadIdx.x] = ctl ? (T)ctl->p[threadIdx.x] : (T)p;
+    __syncthreads();
+    const uint64_t m = sM, v = sV;
+    const uint32_t k = nf;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        cx<T> a;
+        if ((s & m) == v) {
+            a = st[s];
+            for (uint32_t j = 0; j < k; j++) {  // one multiply per collapse, in order
+                a.re = xmul(a.re, pf[j]);
+                a.im = xmul(a.im, pf[j]);
+            }
+        } else {
+            a.re = (T)0;
+            a.im = (T)0;
+        }
+        st[s] = a;
+    }
+}
+
+template <class T>
+cudaError_t launch_collapse(void *st, uint32_t n, const MeasureCtl *ctl, uint64_t M, uint64_t V, double p,
+                            cudaStream_t s) {
+    const uint64_t ns = 1ull << n;
+    uint64_t g = (ns + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_collapse<T><<<(unsigned)g, 256, 0, s>>>((cx<T> *)st, ns, ctl, M, V, p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---- Pauli strings ------------------------------------------------------------
+// <psi|P|psi> with P = i^{nY} X^x Z^z (per qubit).  For x == 0 the sum is
+// sum_s (-1)^{|s & z|} |a_s|^2.  For x != 0 each pair (s, s^x) with bit h
+// (the highest of x) clear contributes +-2 (-1)^{|s & z|} Re or Im of
+// conj(a_s) a_{s^x}; the host folds i^{nY} and (-1)^{|x & z|} into `factor`
+// and `use_im`.
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads)
+    k_pauli_group(const cx<T> *__restrict__ st, uint32_t n, PauliGroup g, ReduceScratch rs) {
+    typename AccOf<T>::type acc[kMaxTerms];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t nt = g.nterms;
+    if (g.x == 0) {
+        const uint64_t count = 1ull << n;
+        for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < count; s += stride) {
+            const cx<T> a = st[s];
+#pragma unroll
+            for (int k = 0; k < kMaxTerms; k++) {
+                if (k < (int)nt) {
+                    if ((__popcll(s & g.z[k]) & 1) ^ (g.factor[k] < 0)) {
+                        acc[k].add_prod_neg(a.re, a.re);
+                        acc[k].add_prod_neg(a.im, a.im);
+                    } else {
+                        acc[k].add_prod(a.re, a.re);
+                        acc[k].add_prod(a.im, a.im);
+                    }
+                }
+            }
+        }
+    } else {
+        const uint32_t h = 63 - __clzll((long long)g.x);
+        const uint64_t count = 1ull << (n - 1);
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+            const uint64_t s = insert_zero(i, h);
+            const cx<T> a = st[s], b = st[s ^ g.x];
+#pragma unroll
+            for (int k = 0; k < kMaxTerms; k++) {
+                if (k < (int)nt) {
+                    const bool neg = (__popcll(s & g.z[k]) & 1) ^ (g.factor[k] < 0);
+                    // Re(conj(a) b) = a.re b.re + a.im b.im ; Im = a.re b.im - a.im b.re
+                    if (!g.use_im[k]) {
+                        if (neg) {
+                            acc[k].add_prod_neg(a.re, b.re);
+                            acc[k].add_prod_neg(a.im, b.im);
+                        } else {
+                            acc[k].add_prod(a.re, b.re);
+                            acc[k].add_prod(a.im, b.im);
+                        }
+                    } else {
+                        if (neg) {
+                            acc[k].add_prod_neg(a.re, b.im);
+                            acc[k].add_prod(a.im, b.re);
+                        } else {
+                            acc[k].add_prod(a.re, b.im);
+                            acc[k].add_prod_neg(a.im, b.re);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    for (int k = 0; k < (int)nt; k++) {
+        const double f = fabs(g.factor[k]);
+        const double v = block_sum(acc[k].value() * f);
+        if (threadIdx.x == 0) rs.partials[(size_t)blockIdx.x * kMaxTerms + k] = v;
+    }
+    if (last_block(rs.ticket)) {
+        for (int k = 0; k < (int)nt; k++) {
+            const double t = sum_partials(rs.partials, gridDim.x, kMaxTerms, k);
+            if (threadIdx.x == 0) rs.result[k] = t;
+        }
+        if (threadIdx.x == 0) *rs.ticket = 0;
+    }
+}
+
+template <class T>
+cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, const ReduceScratch &rs,
+                               cudaStream_t s) {
+    k_pauli_group<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, n, g, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---- support test for dump / sample ---------------------------------------
+// Reference: hypot(re, im) > F(eps) in F (src/dense.rs:374).  With hypot
+// correctly rounded this is re^2 + im^2 > m^2, m the midpoint between F(eps)
+// and the next F value; decided in double with a guard band, and with an
+// exact double evaluation inside the band.
+__device__ __forceinline__ bool above_eps(cx<float> a) {
+    const float q = __fmaf_rn(a.re, a.re, __fmul_rn(a.im, a.im));
+    const float lo = 9.99998e-13f, hi = 1.000002e-12f;  // band around (1e-6)^2
+    if (q > hi) return true;
+    if (q < lo) return false;
+    const double e = (double)1e-6f, e_next = (double)__int_as_float(__float_as_int(1e-6f) + 1);
+    const double mid = 0.5 * (e + e_next);
+    const double x = (double)a.re * (double)a.re + (double)a.im * (double)a.im;
+    return x > mid * mid;
+}
+__device__ __forceinline__ bool above_eps(cx<double> a) {
+    const double q = a.re * a.re + a.im * a.im;
+    return q > 1e-30;
+}
+
+template <class T>
+__device__ __forceinline__ double weight(cx<T> a) {
+    if (!above_eps(a)) return 0.0;
+    const double r = (double)a.re, i = (double)a.im;
+    return __fma_rn(r, r, __dmul_rn(i, i));
+}
+
+int dump_blocks(uint32_t n) {
+    const uint64_t ns = 1ull << n;
+    uint64_t R = ns / 4096;
+    if (R < 256) R = 256;
+    if (R > ns) R = ns;
+    return (int)(ns / R);
+}
+int sample_blocks(uint32_t n) { return dump_blocks(n); }
+
+template <class T>
+__global__ void __launch_bounds__(256) k_dump_count(const cx<T> *__restrict__ st, uint64_t R, uint64_t *counts) {
+    const uint64_t base = (uint64_t)blockIdx.x * R;
+    unsigned c = 0;
+    for (uint64_t i = threadIdx.x; i < R; i += blockDim.x) c += above_eps(st[base + i]) ? 1u : 0u;
+    const double t = block_sum((double)c);
+    if (threadIdx.x == 0) counts[blockIdx.x] = (uint64_t)t;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    k_dump_write(const cx<T> *__restrict__ st, uint64_t R, const uint64_t *offsets, DumpSpec spec, uint64_t *states,
+                 double *re, double *im) {
+    __shared__ unsigned wcount[8];
+    __shared__ uint8_t q[64];
+    if (threadIdx.x < 64) q[threadIdx.x] = spec.qubits[threadIdx.x];
+    const uint64_t base = (uint64_t)blockIdx.x * R;
+    uint64_t running = offsets[blockIdx.x];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    for (uint64_t c0 = 0; c0 < R; c0 += blockDim.x) {
+        const uint64_t i = c0 + threadIdx.x;
+        bool keep = false;
+        cx<T> a{};
+        if (i < R) {
+            a = st[base + i];
+            keep = above_eps(a);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        unsigned before = 0, total = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+            if (k < w) before += wcount[k];
+            total += wcount[k];
+        }
+        if (keep) {
+            const uint64_t pos = running + before + __popc(bal & ((1u << lane) - 1));
+            const uint64_t s = base + i;
+            uint64_t packed = 0;
+            for (uint32_t j = 0; j < spec.nq; j++) packed |= ((s >> q[spec.nq - 1 - j]) & 1ull) << j;
+            states[pos] = packed;
+            re[pos] = (double)a.re;
+            im[pos] = (double)a.im;
+        }
+        running += total;
+        __syncthreads();
+    }
+}
+
+template <class T>
+cudaError_t launch_dump_count(const void *st, uint32_t n, uint64_t *counts, cudaStream_t s) {
+    const int B = dump_blocks(n);
+    const uint64_t R = (1ull << n) / B;
+    k_dump_count<T><<<B, 256, 0, s>>>((const cx<T> *)st, R, counts);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_dump_write(const void *st, uint32_t n, const uint64_t *offsets, const DumpSpec &spec,
+                              uint64_t *states, double *re, double *im, cudaStream_t s) {
+    const int B = dump_blocks(n);
+    const uint64_t R = (1ull << n) / B;
+    k_dump_write<T><<<B, 256, 0, s>>>((const cx<T> *)st, R, offsets, spec, states, re, im);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---- sampling -------------------------------------------------------------------
+// Both kernels walk a block's range in chunks of blockDim with the same scan,
+// so the in-block running sums of the pick kernel end exactly at the block
+// sums the host prefixes.
+template <class T>
+__global__ void __launch_bounds__(256) k_weight_blocksum(const cx<T> *__restrict__ st, uint64_t R, double *blocksum) {
+    const uint64_t base = (uint64_t)blockIdx.x * R;
+    double running = 0.0;
+    for (uint64_t c0 = 0; c0 < R; c0 += blockDim.x) {
+        const uint64_t i = c0 + threadIdx.x;
+        const double w = (i < R) ? weight(st[base + i]) : 0.0;
+        double total;
+        block_inclusive_scan(w, &total);
+        running = running + total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) blocksum[blockIdx.x] = running;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    k_sample_pick(const cx<T> *__restrict__ st, uint64_t R, const uint32_t *blocks, const uint64_t *shot_begin,
+                  const double *prefix, const double *chosen, uint64_t *pick) {
+    __shared__ double pre[256];
+    __shared__ uint64_t last_nz;
+    const uint32_t b = blocks[blockIdx.x];
+    const uint64_t base = (uint64_t)b * R;
+    const double P = prefix[blockIdx.x];
+    uint64_t sh = shot_begin[blockIdx.x];
+    const uint64_t sh_end = shot_begin[blockIdx.x + 1];
+    double running = 0.0;
+    if (threadIdx.x == 0) last_nz = base;
+    __syncthreads();
+    for (uint64_t c0 = 0; c0 < R && sh < sh_end; c0 += blockDim.x) {
+        const uint64_t i = c0 + threadIdx.x;
+        const double w = (i < R) ? weight(st[base + i]) : 0.0;
+        double total;
+        const double incl = block_inclusive_scan(w, &total);
+        pre[threadIdx.x] = P + (running + incl);
+        if (w > 0.0) atomicMax((unsigned long long *)&last_nz, (unsigned long long)(base + i));
+        __syncthreads();
+        const double chunk_end = pre[blockDim.x - 1];
+        // shots whose first prefix above `chosen` lies in this chunk
+        while (sh < sh_end && chosen[sh] < chunk_end) {
+            const uint64_t j = sh + threadIdx.x;
+            if (j < sh_end && chosen[j] < chunk_end) {
+                const double c = chosen[j];
+                int lo = 0, hi = blockDim.x - 1;  // first pre[] > c
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (pre[mid] > c)
+                        hi = mid;
+                    else
+                        lo = mid + 1;
+                }
+                pick[j] = base + c0 + lo;
+            }
+            // advance past every shot resolved in this chunk
+            uint64_t adv = 0;
+            while (sh + adv < sh_end && adv < blockDim.x && chosen[sh + adv] < chunk_end) adv++;
+            sh += adv;
+            __syncthreads();
+        }
+        running = running + total;
+        __syncthreads();
+    }
+    // rounding leftovers: the block's last element with weight
+    for (uint64_t j = sh + threadIdx.x; j < sh_end; j += blockDim.x) pick[j] = last_nz;
+}
+
+template <class T>
+cudaError_t launch_weight_blocksum(const void *st, uint32_t n, double *blocksum, cudaStream_t s) {
+    const int B = sample_blocks(n);
+    const uint64_t R = (1ull << n) / B;
+    k_weight_blocksum<T><<<B, 256, 0, s>>>((const cx<T> *)st, R, blocksum);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_sample_pick(const void *st, uint32_t n, const uint32_t *blocks, uint32_t nblocks_with_shots,
+                               const uint64_t *shot_begin, const double *prefix, const double *chosen,
+                               uint64_t *pick, cudaStream_t s) {
+    const int B = sample_blocks(n);
+    const uint64_t R = (1ull << n) / B;
+    if (nblocks_with_shots == 0) return cudaSuccess;
+    k_sample_pick<T><<<nblocks_with_shots, 256, 0, s>>>((const cx<T> *)st, R, blocks, shot_begin, prefix, chosen,
+                                                          pick);
+    count_launch();
+    return cudaGetLastError();
+}
+
+#define INST(T)                                                                                               \
+    template cudaError_t launch_masked_norm<T>(const void *, uint32_t, uint64_t, uint64_t, const ReduceScratch &, \
+                                               cudaStream_t);                                                 \
+    template cudaError_t launch_measure_step<T>(const void *, uint32_t, MeasureCtl *, uint32_t,                \
+                                                const ReduceScratch &, cudaStream_t);                         \
+    template cudaError_t launch_collapse<T>(void *, uint32_t, const MeasureCtl *, uint64_t, uint64_t, double,   \
+                                            cudaStream_t);                                                    \
+    template cudaError_t launch_pauli_group<T>(const void *, uint32_t, const PauliGroup &, const ReduceScratch &, \
+                                               cudaStream_t);                                                 \
+    template cudaError_t launch_dump_count<T>(const void *, uint32_t, uint64_t *, cudaStream_t);               \
+    template cudaError_t launch_dump_write<T>(const void *, uint32_t, const uint64_t *, const DumpSpec &,        \
+                                              uint64_t *, double *, double *, cudaStream_t);                  \
+    template cudaError_t launch_weight_blocksum<T>(const void *, uint32_t, double *, cudaStream_t);            \
+    template cudaError_t launch_sample_pick<T>(const void *, uint32_t, const uint32_t *, uint32_t,             \
+                                               const uint64_t *, const double *, const double *, uint64_t *,  \
+                                               cudaStream_t);
+INST(float)
+INST(double)
+
+}  // namespace kbwg

@@ -1,0 +1,87 @@
+// Host side of the engine: one handle = one state vector on one GPU.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace kbwg {
+
+// Grow-only device buffer owned by a handle.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+};
+
+// CUDA-event timing of gate-kernel launches on the handle's stream.
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    double bytes = 0.0;
+    cudaError_t mark(cudaStream_t s) {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) return r;
+            pool.push_back(e);
+        }
+        return cudaEventRecord(pool[used++], s);
+    }
+    void release() {
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+        pool.clear();
+        used = 0;
+    }
+};
+
+struct Sim {
+    uint32_t n = 0;
+    int prec = 0;  // 0: complex64, 1: complex128
+    uint32_t flags = 0;
+    int device = 0;
+    uint64_t ns = 0;
+    size_t elem = 0;
+    void *state = nullptr;
+    cudaStream_t stream = nullptr;
+
+    std::vector<GateDesc> queue;  // gates waiting for the next flush
+
+    void *scratch = nullptr;  // reductions + measurement control
+    ReduceScratch rs{};
+    MeasureCtl *d_ctl = nullptr;
+    int *d_err = nullptr;         // set by a kernel whose bounded wait ran out
+    MeasureCtl *h_ctl = nullptr;  // pinned mirror
+    double *h_result = nullptr;   // pinned, kMaxTerms entries
+    DevBuf tmp0, tmp1, tmp2, tmp3, tmp4, tmp5;
+
+    uint64_t rng = 0;  // splitmix64 state of the handle's own draw generator
+
+    Profiler prof;
+
+    // statistics of the last flush
+    uint64_t last_passes = 0;
+    uint64_t last_gates = 0;
+};
+
+// Build the descriptor of one trait gate: constants computed in the state
+// precision exactly as kbw Dense<F> does (src/dense.rs:211-334).
+GateDesc make_gate_desc(int prec, uint32_t kind, uint32_t target, uint64_t ctrl, double angle);
+
+// Run every queued gate (fused sweeps unless KBWG_FLAG_NO_FUSION).
+cudaError_t flush_queue(Sim &s);
+
+// Fusion planner entry used by flush_queue (sweep.cu).
+cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
+
+double next_draw(Sim &s);
+double host_uniform_scale(double total);
+
+}  // namespace kbwg

@@ -1,0 +1,248 @@
+"""Python mirror of the reference's backend trait over the C ABI.
+
+``DenseGB300`` exposes the methods of kbw's ``QuantumExecution`` trait
+(src/quantum_execution.rs:48-162) with the same names and argument meaning:
+gates take ``(target, control)`` or ``(angle, target, control)``,
+``measure_p1`` does not collapse, ``measure_collapse`` takes
+``p = 1/sqrt(P)``, ``dump`` packs ``qubits[0]`` as the most significant bit.
+The ``QubitManager`` level (src/quantum_execution.rs:272-306) is ``measure``,
+``sample`` and ``exp_value`` with explicit uniform draws.
+
+Every call goes to the CUDA engine; nothing here computes amplitudes.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .circuits import PAULI_X, PAULI_Y, PAULI_Z  # noqa: F401
+
+_DT = {"c64": (N.C64, np.complex64), "c128": (N.C128, np.complex128)}
+
+
+def _sizes(seq):
+    a = np.ascontiguousarray(np.asarray(list(seq), dtype=np.uintp))
+    return a
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t)) if a.size else None
+
+
+class DenseGB300:
+    """One state vector of 2^n amplitudes on the current CUDA device."""
+
+    def __init__(self, num_qubits, prec="c128", fusion=True, fast_c128=False, exact_order=False):
+        lib = N.load()
+        if prec not in _DT:
+            raise ValueError("prec must be 'c64' or 'c128'")
+        self.num_qubits = int(num_qubits)
+        self.prec = prec
+        flags = (0 if fusion else N.FLAG_NO_FUSION) | (N.FLAG_FAST_C128 if fast_c128 else 0)
+        flags |= N.FLAG_EXACT_ORDER if exact_order else 0
+        h = ctypes.c_void_p()
+        N.check(lib.kbwg_new(self.num_qubits, _DT[prec][0], flags, ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.kbwg_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- trait gates --------------------------------------------------------------
+    def _g(self, fn, target, control, angle=None):
+        c = _sizes(control)
+        cp = _p(c, ctypes.c_size_t)
+        if angle is None:
+            N.check(fn(self._h, int(target), cp, c.size))
+        else:
+            N.check(fn(self._h, float(angle), int(target), cp, c.size))
+
+    def pauli_x(self, target, control=()):
+        self._g(self._lib.kbwg_pauli_x, target, control)
+
+    def pauli_y(self, target, control=()):
+        self._g(self._lib.kbwg_pauli_y, target, control)
+
+    def pauli_z(self, target, control=()):
+        self._g(self._lib.kbwg_pauli_z, target, control)
+
+    def hadamard(self, target, control=()):
+        self._g(self._lib.kbwg_hadamard, target, control)
+
+    def phase(self, angle, target, control=()):
+        self._g(self._lib.kbwg_phase, target, control, angle)
+
+    def rx(self, angle, target, control=()):
+        self._g(self._lib.kbwg_rx, target, control, angle)
+
+    def ry(self, angle, target, control=()):
+        self._g(self._lib.kbwg_ry, target, control, angle)
+
+    def rz(self, angle, target, control=()):
+        self._g(self._lib.kbwg_rz, target, control, angle)
+
+    def apply(self, circuit):
+        """Queue a list of (kind, target, controls, angle) gates in one call."""
+        arr = (N.Gate * max(len(circuit), 1))()
+        for i, (kind, t, ctrl, ang) in enumerate(circuit):
+            m = 0
+            for c in ctrl:
+                m |= 1 << int(c)
+            arr[i] = N.Gate(int(kind), int(t), m, float(ang))
+        N.check(self._lib.kbwg_apply_gates(self._h, arr, len(circuit)))
+
+    def flush(self):
+        N.check(self._lib.kbwg_flush(self._h))
+
+    # -- measurement ------------------------------------------------------------
+    def measure_p1(self, target):
+        out = ctypes.c_double()
+        N.check(self._lib.kbwg_measure_p1(self._h, int(target), ctypes.byref(out)))
+        return out.value
+
+    def measure_collapse(self, target, result, p):
+        N.check(self._lib.kbwg_measure_collapse(self._h, int(target), bool(result), float(p)))
+
+    def measure(self, qubits, draws=None):
+        q = _sizes(qubits)
+        d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
+        if d is not None and d.size < q.size:
+            raise ValueError("one draw per qubit is needed")
+        out = ctypes.c_uint64()
+        N.check(self._lib.kbwg_measure(self._h, _p(q, ctypes.c_size_t), q.size,
+                                       None if d is None else _p(d, ctypes.c_double), ctypes.byref(out)))
+        return int(out.value)
+
+    def dump(self, qubits):
+        q = _sizes(qubits)
+        size = ctypes.c_size_t()
+        N.check(self._lib.kbwg_dump(self._h, _p(q, ctypes.c_size_t), q.size, None, None, None, 0,
+                                    ctypes.byref(size)))
+        m = size.value
+        st = np.zeros(max(m, 1), np.uint64)
+        re = np.zeros(max(m, 1), np.float64)
+        im = np.zeros(max(m, 1), np.float64)
+        N.check(self._lib.kbwg_dump(self._h, _p(q, ctypes.c_size_t), q.size, _p(st, ctypes.c_uint64),
+                                    _p(re, ctypes.c_double), _p(im, ctypes.c_double), m, ctypes.byref(size)))
+        return st[:m], re[:m], im[:m]
+
+    def sample(self, qubits, shots, draws=None):
+        q = _sizes(qubits)
+        shots = int(shots)
+        d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
+        if d is not None and d.size < shots:
+            raise ValueError("one draw per shot is needed")
+        st = np.zeros(max(shots, 1), np.uint64)
+        ct = np.zeros(max(shots, 1), np.uint64)
+        n = ctypes.c_size_t()
+        N.check(self._lib.kbwg_sample(self._h, _p(q, ctypes.c_size_t), q.size, shots,
+                                      None if d is None else _p(d, ctypes.c_double),
+                                      _p(st, ctypes.c_uint64), _p(ct, ctypes.c_uint64), max(shots, 1),
+                                      ctypes.byref(n)))
+        return st[:n.value], ct[:n.value]
+
+    def exp_value(self, hamiltonian):
+        """hamiltonian: list of (coefficient, [(pauli_code, qubit), ...])."""
+        paulis, qubits, offsets, coefs = [], [], [0], []
+        for coef, terms in hamiltonian:
+            for p, q in terms:
+                paulis.append(int(p))
+                qubits.append(int(q))
+            offsets.append(len(paulis))
+            coefs.append(float(coef))
+        pa = np.ascontiguousarray(paulis if paulis else [0], dtype=np.uint8)
+        qa = np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp)
+        oa = np.ascontiguousarray(offsets, dtype=np.uintp)
+        ca = np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64)
+        out = ctypes.c_double()
+        N.check(self._lib.kbwg_exp_value(self._h, _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t),
+                                         _p(oa, ctypes.c_size_t), _p(ca, ctypes.c_double), len(coefs),
+                                         ctypes.byref(out)))
+        return out.value
+
+    def clear(self):
+        N.check(self._lib.kbwg_clear(self._h))
+
+    # -- raw access -----------------------------------------------------------------
+    def state(self):
+        dt = _DT[self.prec][1]
+        out = np.zeros(1 << self.num_qubits, dt)
+        N.check(self._lib.kbwg_get_state(self._h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
+        return out
+
+    def set_state(self, amps):
+        a = np.ascontiguousarray(np.asarray(amps, dtype=_DT[self.prec][1]))
+        if a.size != 1 << self.num_qubits:
+            raise ValueError("need 2^n amplitudes")
+        N.check(self._lib.kbwg_set_state(self._h, a.ctypes.data_as(ctypes.c_void_p), a.nbytes))
+
+    def swap_qubits(self, a, b):
+        N.check(self._lib.kbwg_swap_qubits(self._h, int(a), int(b)))
+
+    def device_info(self):
+        n = ctypes.c_size_t()
+        prec = ctypes.c_int32()
+        ptr = ctypes.c_void_p()
+        nbytes = ctypes.c_size_t()
+        N.check(self._lib.kbwg_state_info(self._h, ctypes.byref(n), ctypes.byref(prec), ctypes.byref(ptr),
+                                          ctypes.byref(nbytes)))
+        return int(n.value), int(prec.value), int(ptr.value or 0), int(nbytes.value)
+
+    def stream_handle(self):
+        ptr = ctypes.c_void_p()
+        N.check(self._lib.kbwg_stream(self._h, ctypes.byref(ptr)))
+        return int(ptr.value or 0)
+
+    def profile(self, enable=True):
+        N.check(self._lib.kbwg_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        n = ctypes.c_uint64()
+        ms = ctypes.c_double()
+        b = ctypes.c_double()
+        N.check(self._lib.kbwg_profile_read(self._h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
+        return int(n.value), float(ms.value), float(b.value)
+
+    def last_flush_stats(self):
+        g = ctypes.c_uint64()
+        p = ctypes.c_uint64()
+        N.check(self._lib.kbwg_last_flush_stats(self._h, ctypes.byref(g), ctypes.byref(p)))
+        return int(g.value), int(p.value)
+
+
+def plan(num_qubits, circuit, prec="c128", exact_order=False):
+    """Host planner diagnostic: list of (tile_mask, [gate indices in execution order])."""
+    lib = N.load()
+    n = len(circuit)
+    arr = (N.Gate * max(n, 1))()
+    for i, (kind, t, ctrl, ang) in enumerate(circuit):
+        m = 0
+        for c in ctrl:
+            m |= 1 << int(c)
+        arr[i] = N.Gate(int(kind), int(t), m, float(ang))
+    order = (ctypes.c_uint32 * max(n, 1))()
+    ends = (ctypes.c_uint32 * max(n, 1))()
+    masks = (ctypes.c_uint64 * max(n, 1))()
+    ns = ctypes.c_size_t()
+    flags = N.FLAG_EXACT_ORDER if exact_order else 0
+    N.check(lib.kbwg_plan(int(num_qubits), _DT[prec][0], flags, arr, n, order, ends, masks, ctypes.byref(ns)))
+    out, b = [], 0
+    for k in range(ns.value):
+        e = ends[k]
+        out.append((int(masks[k]), [int(order[i]) for i in range(b, e)]))
+        b = e
+    return out

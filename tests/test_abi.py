@@ -1,0 +1,104 @@
+"""CPU tests of the C ABI library: it loads, exports every symbol declared in
+include/kbwg.h, and its host-side fusion planner only reorders gates that
+commute (checked by replaying the planned order on the oracle)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from kbw_gb300 import _native as N
+from kbw_gb300 import circuits as C
+from kbw_gb300 import plan
+from conftest import ROOT, rel_err
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "kbwg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(kbwg_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(N.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return N.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = header_functions()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(N.SIGNATURES), set(names) ^ set(N.SIGNATURES)
+
+
+def test_build_info(lib):
+    assert N.build_info().startswith("kbw-gb300")
+
+
+def test_new_without_gpu_fails_cleanly(lib, cuda_available):
+    if cuda_available:
+        pytest.skip("GPU present")
+    import ctypes
+    h = ctypes.c_void_p()
+    code = lib.kbwg_new(4, N.C64, 0, ctypes.byref(h))
+    assert code != N.OK and not h.value
+    assert lib.kbwg_new(33, N.C64, 0, ctypes.byref(h)) == N.EQUBITS
+
+
+def replay(n, circuit, prec):
+    """Execute the planner's order on the oracle."""
+    sweeps = plan(n, circuit, prec)
+    order = [i for _, idx in sweeps for i in idx]
+    assert sorted(order) == list(range(len(circuit)))
+    o = oracle.OracleDense(n, prec)
+    o.apply([circuit[i] for i in order])
+    return o, sweeps
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_planner_order_is_equivalent(lib, prec, seed):
+    n = 14
+    circ = C.random_circuit(n, 300, seed, max_controls=3)
+    ref = oracle.OracleDense(n, prec)
+    ref.apply(circ)
+    o, sweeps = replay(n, circ, prec)
+    # only commuting gates are reordered, so the states agree to rounding
+    assert rel_err(o.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
+    K = 13 if prec == "c64" else 12
+    for mask, idx in sweeps:
+        assert bin(mask).count("1") == K
+        assert mask & 0b11111 == 0b11111
+        for i in idx:
+            kind, t, _, _ = circ[i]
+            if kind not in (C.Z, C.P, C.RZ):
+                assert (mask >> t) & 1
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_planner_exact_order_keeps_program_order(lib, prec):
+    n = 15
+    circ = C.random_circuit(n, 250, 4, max_controls=2)
+    sweeps = plan(n, circ, prec, exact_order=True)
+    order = [i for _, idx in sweeps for i in idx]
+    assert order == list(range(len(circ)))
+    assert len(sweeps) < len(circ) // 3
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_planner_brickwork_sweep_count(lib, prec):
+    circ = C.brickwork(30, 20, 0)
+    sweeps = plan(30, circ, prec)
+    order = [i for _, idx in sweeps for i in idx]
+    assert sorted(order) == list(range(len(circ)))
+    # 25 high qubits per layer over 8 (c64) / 7 (c128) high slots per tile
+    assert len(sweeps) <= (70 if prec == "c64" else 80), len(sweeps)
+    o16, _ = replay(16, C.brickwork(16, 6, 3), prec)
+    ref = oracle.OracleDense(16, prec)
+    ref.apply(C.brickwork(16, 6, 3))
+    assert rel_err(o16.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)

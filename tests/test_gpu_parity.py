@@ -1,0 +1,290 @@
+"""GPU parity: the CUDA engine against the oracle (restated kbw Dense<F>).
+
+Gate arithmetic keeps the reference's per-amplitude operation order, so with
+the order-preserving planner (exact_order=True) and with fusion off the
+amplitudes must equal the oracle's exactly (value equality), in both
+precisions.  The default planner also reorders gates that commute, which
+changes rounding only: complex128 amplitudes then agree within 1e-12
+relative (the parity bar) and complex64 within 1e-5.  Reductions accumulate
+in FP64, so p1 and <H> agree within 1e-12 (c128) / 1e-6 (c64); measurement
+outcomes and sampled bitstrings are identical given the same draws.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from kbw_gb300 import DenseGB300, KbwgError
+from kbw_gb300 import circuits as C
+from conftest import decode_circuit, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["c128", "c64"]
+
+
+TOL = {"c128": 1e-12, "c64": 1e-5}
+
+
+def both(n, circ, prec, fusion=True, exact_order=True):
+    sim = DenseGB300(n, prec, fusion=fusion, exact_order=exact_order)
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, prec)
+    ref.apply(circ)
+    return sim, ref
+
+
+def assert_exact(sim, ref):
+    got = sim.state().astype(np.complex128)
+    want = ref.state()
+    if not np.array_equal(got, want):
+        bad = np.flatnonzero(got != want)
+        raise AssertionError("%d amplitudes differ, first at %d: %r vs %r (rel %.3g)"
+                             % (bad.size, bad[0], got[bad[0]], want[bad[0]], rel_err(got, want)))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("fusion", [True, False])
+def test_every_gate_kind_small_registers(prec, fusion):
+    for n in range(1, 15):
+        circ = C.random_circuit(n, 12 * n, 100 + n, max_controls=min(3, n - 1))
+        sim, ref = both(n, circ, prec, fusion)
+        assert_exact(sim, ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n,gates,seed", [(16, 400, 1), (18, 500, 2), (20, 600, 3), (21, 300, 4)])
+def test_fused_sweeps_exact(prec, n, gates, seed):
+    circ = C.random_circuit(n, gates, seed, max_controls=3)
+    sim, ref = both(n, circ, prec, exact_order=True)
+    assert_exact(sim, ref)
+    _, passes = sim.last_flush_stats()
+    assert passes < gates
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n,gates,seed", [(16, 400, 1), (20, 600, 3), (22, 400, 5)])
+def test_fused_sweeps_reordered(prec, n, gates, seed):
+    circ = C.random_circuit(n, gates, seed, max_controls=3)
+    sim, ref = both(n, circ, prec, exact_order=False)
+    assert rel_err(sim.state(), ref.state()) < TOL[prec]
+    if prec == "c64":  # against the complex128 oracle: state infidelity (norms divided out)
+        r128 = oracle.OracleDense(n, "c128")
+        r128.apply(circ)
+        a, b = r128.state(), sim.state().astype(np.complex128)
+        ov = abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
+        assert 1 - ov < 1e-8
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("exact_order", [True, False])
+def test_brickwork(prec, exact_order):
+    circ = C.brickwork(20, 8, 0)
+    sim, ref = both(20, circ, prec, exact_order=exact_order)
+    if exact_order:
+        assert_exact(sim, ref)
+    else:
+        assert rel_err(sim.state(), ref.state()) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_single_gate_every_target_and_control(prec):
+    n = 15
+    rng = np.random.default_rng(7)
+    base = C.random_circuit(n, 40, 8, max_controls=1)
+    for kind in range(8):
+        for t in range(n):
+            c = int(rng.integers(0, n - 1))
+            c = c if c < t else c + 1
+            angle = float(rng.uniform(0, 2 * math.pi))
+            circ = base + [(kind, t, (c,), angle), (kind, (t + 3) % n, (), angle)]
+            sim, ref = both(n, circ, prec)
+            assert_exact(sim, ref)
+
+
+def test_random_small_golden():
+    g = load_golden("random_small.npz")
+    for i in range(int(g["count"])):
+        n = int(g["c%d_n" % i])
+        sim = DenseGB300(n, "c128")
+        sim.apply(decode_circuit(g, "c%d" % i))
+        assert rel_err(sim.state(), g["c%d_state" % i]) < 1e-12
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grover12(prec):
+    g = load_golden("grover12.npz")
+    tol = 1e-12 if prec == "c128" else 1e-4
+    for seed in range(3):
+        m = C.grover_marked(seed)
+        sim = DenseGB300(12, prec)
+        sim.apply(C.grover(12, m, 50))
+        prob = np.abs(sim.state().astype(np.complex128)) ** 2
+        assert np.max(np.abs(prob - g["prob_seed%d" % seed])) < tol
+        assert abs(prob[m] - C.grover_success_probability(12, 50)) < tol
+    sim = DenseGB300(12, "c128")
+    sim.apply(C.grover(12, C.grover_marked(0), 50))
+    st, ct = sim.sample(list(range(12)), 1024, g["sample_draws"])
+    assert np.array_equal(st, g["sample_states"]) and np.array_equal(ct, g["sample_counts"])
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_measure_p1_and_collapse(prec):
+    n = 16
+    circ = C.random_circuit(n, 200, 11, max_controls=2)
+    sim, ref = both(n, circ, prec)
+    tol = 1e-12 if prec == "c128" else 2e-6
+    for t in (0, 3, 9, 15):
+        assert abs(sim.measure_p1(t) - ref.measure_p1(t)) < tol
+    p1 = ref.measure_p1(9)
+    p = 1.0 / math.sqrt(p1)
+    sim.measure_collapse(9, True, p)
+    ref.measure_collapse(9, True, p)
+    assert_exact(sim, ref)
+    sim.measure_collapse(2, False, 1.25)
+    ref.measure_collapse(2, False, 1.25)
+    assert_exact(sim, ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [5, 13, 17])
+def test_measure_with_draws(prec, n):
+    for rep in range(4):
+        circ = C.random_circuit(n, 15 * n, 40 + rep, max_controls=2)
+        sim, ref = both(n, circ, prec)
+        qubits = list(range(n)) if rep % 2 == 0 else [n - 1, 0, n // 2]
+        draws = C.uniform_draws(len(qubits), 70 + rep)
+        assert sim.measure(qubits, draws) == ref.measure(qubits, draws)
+        tol = 1e-12 if prec == "c128" else 1e-5
+        assert rel_err(sim.state(), ref.state()) < tol
+
+
+def test_measure_golden():
+    g = load_golden("measure.npz")
+    for i in range(int(g["count"])):
+        n = int(g["m%d_n" % i])
+        qubits = [int(q) for q in g["m%d_qubits" % i]]
+        sim = DenseGB300(n, "c128")
+        sim.apply(decode_circuit(g, "m%d" % i))
+        st, ct = sim.sample(qubits, 256, g["m%d_sdraws" % i])
+        assert np.array_equal(st, g["m%d_sstates" % i]) and np.array_equal(ct, g["m%d_scounts" % i])
+        assert sim.measure(qubits, g["m%d_draws" % i]) == int(g["m%d_result" % i])
+        assert rel_err(sim.state(), g["m%d_post" % i]) < 1e-12
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [3, 12, 18])
+def test_dump_exact(prec, n):
+    circ = C.random_circuit(n, 6 * n, 21 + n, max_controls=2, kinds=[C.H, C.X, C.RY, C.P])
+    sim, ref = both(n, circ, prec)
+    for qubits in (list(range(n)), [n - 1, 0], list(range(n))[::-1][: max(1, n // 2)]):
+        a = sim.dump(qubits)
+        b = ref.dump(qubits)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n", [4, 14, 19])
+def test_sample_bit_exact(prec, n):
+    circ = C.random_circuit(n, 10 * n, 31 + n, max_controls=2)
+    sim, ref = both(n, circ, prec)
+    shots = 2048
+    draws = C.uniform_draws(shots, 5 + n)
+    for qubits in (list(range(n)), [0, n - 1]):
+        st, ct = sim.sample(qubits, shots, draws)
+        so, co = ref.sample(qubits, shots, draws)
+        assert np.array_equal(st, so) and np.array_equal(ct, co)
+        assert int(ct.sum()) == shots
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_exp_value(prec):
+    tol = 1e-11 if prec == "c128" else 2e-5
+    for n, L, seed in [(6, 3, 1), (12, 2, 2), (16, 3, 3)]:
+        params = C.hea_params(n, L, seed)
+        sim, ref = both(n, C.hea(n, L, params), prec)
+        h = C.tfim_ring(n)
+        assert abs(sim.exp_value(h) - ref.exp_value(h)) < tol * n
+        mixed = [(0.7, [(C.PAULI_Y, 0), (C.PAULI_X, n - 1)]), (-1.3, [(C.PAULI_Y, 1)]),
+                 (0.25, [(C.PAULI_Z, 2), (C.PAULI_Y, 3), (C.PAULI_X, 0)]),
+                 (1.1, [(C.PAULI_Y, 2), (C.PAULI_Y, 4), (C.PAULI_Y, 5)]), (2.0, [])]
+        assert abs(sim.exp_value(mixed) - ref.exp_value(mixed)) < tol * 10
+    g = load_golden("expval.npz")
+    for i in range(int(g["count"])):
+        n, L = int(g["e%d_n" % i]), int(g["e%d_L" % i])
+        sim = DenseGB300(n, "c128")
+        sim.apply(C.hea(n, L, g["e%d_params" % i]))
+        assert abs(sim.exp_value(C.tfim_ring(n)) - float(g["e%d_tfim" % i])) < 1e-11 * n
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_swap_qubits_exact(prec):
+    n = 15
+    circ = C.random_circuit(n, 100, 77, max_controls=2)
+    sim, ref = both(n, circ, prec)
+    for a, b in [(0, 14), (3, 4), (13, 2)]:
+        sim.swap_qubits(a, b)
+        ref.swap_qubits(a, b)
+        assert_exact(sim, ref)
+
+
+def test_clear_and_state_roundtrip():
+    sim = DenseGB300(10, "c128")
+    sim.apply(C.random_circuit(10, 50, 3))
+    sim.clear()
+    s = sim.state()
+    assert s[0] == 1 and np.count_nonzero(s) == 1
+    rng = np.random.default_rng(0)
+    v = rng.normal(size=1024) + 1j * rng.normal(size=1024)
+    sim.set_state(v)
+    assert np.array_equal(sim.state(), v)
+
+
+def test_errors_are_status_codes():
+    with pytest.raises(KbwgError) as e:
+        DenseGB300(33, "c64")
+    assert e.value.code == 2
+    sim = DenseGB300(4, "c64")
+    with pytest.raises(KbwgError):
+        sim.pauli_x(4)
+    with pytest.raises(KbwgError):
+        sim.pauli_x(1, [1])
+    with pytest.raises(KbwgError):
+        sim.exp_value([(1.0, [(C.PAULI_X, 0), (C.PAULI_Z, 0)])])
+    sim.pauli_x(0)
+    # qubits[0] is the most significant bit of the packed result
+    assert sim.measure([0, 1], [0.5, 0.5]) == 0b10
+
+
+def test_zero_qubits():
+    sim = DenseGB300(0, "c128")
+    assert sim.state().tolist() == [1]
+    assert sim.measure([], []) == 0
+    st, re, im = sim.dump([])
+    assert st.tolist() == [0] and re.tolist() == [1.0]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_28q_brickwork_round_trip(prec):
+    """Size-independent properties at a large register: the norm stays 1 and
+    the inverse circuit returns |0...0>."""
+    n = 28
+    circ = C.brickwork(n, 6, 5)
+    inv = []
+    for kind, t, c, a in reversed(circ):
+        if kind in (C.P, C.RX, C.RY, C.RZ):
+            inv.append((kind, t, c, -a))
+        elif kind == C.Y:
+            inv.append((kind, t, c, a))
+        else:
+            inv.append((kind, t, c, a))
+    sim = DenseGB300(n, prec)
+    sim.apply(circ)
+    z = sim.exp_value([(1.0, [])])
+    assert abs(z - 1.0) < (1e-12 if prec == "c128" else 1e-5)
+    sim.apply(inv)
+    st, re, im = sim.dump(list(range(n)))
+    tol = 1e-12 if prec == "c128" else 1e-4
+    assert st[0] == 0 and abs(re[0] - 1.0) < tol
