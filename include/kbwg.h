@@ -204,6 +204,27 @@ int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h);
 /* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
 int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
 
+/* ---- allocation-free entry (no counterpart in the reference) ------------- */
+
+/* For callers that cannot allocate device memory: code recorded into a CUDA
+ * graph (cudaMalloc cannot be captured), plugins whose host runtime owns all
+ * device allocations, real-time loops that cannot absorb an allocation's
+ * implicit synchronisation.  Writes to *out (device memory, one double) the
+ * sum of |a_s|^2 over the basis states s with (s & mask) == value -- with
+ * mask = value = 1 << t that is kbwg_measure_p1(t) -- for the caller's state
+ * (device pointer, 2^num_qubits interleaved amplitudes in `precision`),
+ * launched on `stream` (NULL: the legacy default stream) without waiting.
+ * It calls no cudaMalloc/cudaFree and no allocating library routine: its
+ * scratch is a fixed 8 KiB device array in this library (608 partial sums
+ * and a ticket), held by every GPU that loads the library until exit.
+ * Limits: num_qubits <= 32 (KBWG_EQUBITS otherwise); value must lie inside
+ * mask (KBWG_EINVAL).  The first call on a device looks up the array's device
+ * address with that device current (kbwg_select_device), so make it before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (other streams, other threads) race; serialise them. */
+int32_t kbwg_masked_norm_noalloc(const void *state, uintptr_t num_qubits, int32_t precision,
+                                 uint64_t mask, uint64_t value, double *out, void *stream);
+
 /* Text of the last error on this thread ("" if none). */
 const char *kbwg_last_error(void);
 

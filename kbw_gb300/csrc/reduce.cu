@@ -8,6 +8,9 @@
 // double per thread before the block tree.
 #include <float.h>
 
+#include <mutex>
+
+#include "../../include/kbwg.h"
 #include "kernels.h"
 
 namespace kbwg {
@@ -570,6 +573,90 @@ cudaError_t launch_sample_pick(const void *st, uint32_t n, const uint32_t *block
     count_launch();
     return cudaGetLastError();
 }
+
+// ---- allocation-free masked norm ----------------------------------------------
+// Some callers of this library cannot allocate device memory: code that runs
+// while a CUDA graph is being captured (cudaMalloc is not capturable), plugins
+// hosted by a runtime that owns every device allocation through its own pool,
+// and real-time loops that cannot take the implicit synchronisation of an
+// allocation.  kbwg_masked_norm_noalloc serves them: it runs the same
+// reduction as kbwg_measure_p1 but keeps its scratch (608 per-block partial
+// sums and the last-block ticket) in the fixed device array below instead of
+// a per-handle cudaMalloc.  Every GPU that loads this library holds the array
+// (8 KiB) until the process exits.
+constexpr size_t kNoAllocScratchBytes = 8192;
+constexpr size_t kNoAllocTicketOffset = 4864;  // after kReduceBlocks doubles, 256-aligned
+static_assert(kReduceBlocks * sizeof(double) <= kNoAllocTicketOffset, "partials overflow the fixed scratch");
+static_assert(kNoAllocTicketOffset + 256 <= kNoAllocScratchBytes, "ticket overflows the fixed scratch");
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Host code may not use g_noalloc_scratch as an address (it names a host-side
+// stand-in); the device address is looked up once per device.
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[256];
+
+static cudaError_t noalloc_scratch(void **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace kbwg
+
+extern "C" int32_t kbwg_masked_norm_noalloc(const void *state, uintptr_t num_qubits, int32_t precision,
+                                            uint64_t mask, uint64_t value, double *out, void *stream) {
+    using namespace kbwg;
+    if (!state || !out) {
+        set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: null state or output pointer");
+        return KBWG_EINVAL;
+    }
+    if (num_qubits > 32) {
+        set_error(KBWG_EQUBITS, "kbwg_masked_norm_noalloc: at most 32 qubits (its fixed scratch serves "
+                                "a 608-block grid over up to 2^32 amplitudes)");
+        return KBWG_EQUBITS;
+    }
+    if (precision != KBWG_C64 && precision != KBWG_C128) {
+        set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: bad precision");
+        return KBWG_EINVAL;
+    }
+    const uint64_t all = (num_qubits >= 64) ? ~0ull : ((1ull << num_qubits) - 1);
+    if ((mask & ~all) || (value & ~mask)) {
+        set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: mask/value outside the register or value outside mask");
+        return KBWG_EINVAL;
+    }
+    void *base = nullptr;
+    cudaError_t e = noalloc_scratch(&base);
+    if (e != cudaSuccess) {
+        set_error(KBWG_ECUDA, std::string("kbwg_masked_norm_noalloc: scratch lookup: ") + cudaGetErrorString(e));
+        return KBWG_ECUDA;
+    }
+    ReduceScratch rs;
+    rs.partials = (double *)base;
+    rs.ticket = (unsigned *)((char *)base + kNoAllocTicketOffset);
+    rs.result = out;
+    cudaStream_t s = (cudaStream_t)stream;
+    e = cudaMemsetAsync(rs.ticket, 0, sizeof(unsigned), s);  // the array keeps the last call's contents
+    if (e == cudaSuccess)
+        e = precision ? launch_masked_norm<double>(state, (uint32_t)num_qubits, mask, value, rs, s)
+                      : launch_masked_norm<float>(state, (uint32_t)num_qubits, mask, value, rs, s);
+    if (e != cudaSuccess) {
+        set_error(KBWG_ECUDA, std::string("kbwg_masked_norm_noalloc: ") + cudaGetErrorString(e));
+        return KBWG_ECUDA;
+    }
+    return KBWG_OK;
+}
+
+namespace kbwg {
 
 #define INST(T)                                                                                               \
     template cudaError_t launch_masked_norm<T>(const void *, uint32_t, uint64_t, uint64_t, const ReduceScratch &, \
