@@ -196,6 +196,26 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(sim, circ, steps, warmup, torch):
+    """CUDA-event time of `steps` circuit applications on the engine's stream."""
+    for _ in range(warmup):
+        sim.apply(circ)
+        sim.flush()
+    ext = torch.cuda.ExternalStream(sim.stream_handle())
+    sim.profile(True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        sim.apply(circ)
+        sim.flush()
+    e1.record(ext)
+    torch.cuda.synchronize()
+    nl, kms, kbytes = sim.profile_read()
+    sim.profile(False)
+    return e0.elapsed_time(e1) / steps, nl, kms, kbytes
+
+
 def run_ours(args, world, rank, local):
     import torch
     import kbw_gb300
@@ -207,12 +227,14 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     N.select_device(local)
     n, prec = args.qubits, args.prec
+    fast = prec == "c128" and args.arith == "ff"
     B = 16 if prec == "c128" else 8
     circ = C.brickwork(n, args.layers, 0)
     G = len(circ)
     step_bytes = G * 2 * B * (1 << n)
+    peak, peak_kind = load_peaks()
 
-    sim = DenseGB300(n, prec)
+    sim = DenseGB300(n, prec, fast_c128=fast)
     ext = torch.cuda.ExternalStream(sim.stream_handle())
 
     def step():
@@ -245,12 +267,12 @@ def run_ours(args, world, rank, local):
     ms_step = ms / args.steps
     value = world * step_bytes / (ms_step * 1e-3) / 1e9
 
-    peak, peak_kind = load_peaks()
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else None
+    kname = "k_sweep<%s>" % ({"c64": "Exact<float>", "c128": "FFPol" if fast else "Exact<double>"}[prec])
     roofline = {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None, "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                "traffic": args.traffic, "kernel": "k_sweep<%s>" % ("double" if prec == "c128" else "float"),
-                "launches": nl, "avg_launch_ms": round(kms / max(nl, 1), 4), "peak_source": peak_kind + " hbm_gbs"}
+                "traffic": args.traffic, "kernel": kname, "launches": nl,
+                "avg_launch_ms": round(kms / max(nl, 1), 4), "peak_source": peak_kind + " hbm_gbs (burst copy)"}
 
     # ---- e2e through the C ABI, host buffers ----
     zs = [(1.0, [(C.PAULI_Z, q)]) for q in range(n)]
@@ -281,34 +303,41 @@ def run_ours(args, world, rank, local):
            "h2d_bytes_per_step": (h1 - h0) // args.e2e_steps, "d2h_bytes_per_step": (d1 - d0) // args.e2e_steps,
            "ms_per_step": round(e2e_s * 1e3, 2),
            "calls": "clear + %d gate calls + exp_value(%d Z_i) + measure(%d qubits)" % (G, n, n)}
-    sim.close()
-    del sim
 
-    # ---- secondary: the same circuit in complex64 ----
     secondary = {}
     if args.secondary and prec == "c128":
+        # parity of the headline arithmetic at full size: one circuit from |0>
+        # in float-float and in binary64, compared on the device
+        exact = DenseGB300(n, "c128")
+        exact.apply(circ)
+        exact.flush()
+        if fast:
+            sim.clear()
+            sim.apply(circ)
+            sim.flush()
+            secondary["parity_vs_binary64"] = {"relative_l2": sim.distance(exact),
+                                               "circuit": "one application from |0>"}
+        sim.close()
+        del sim
+        ms_x, nlx, kmsx, kbx = time_steps(exact, circ, 1, 0, torch)
+        achx = kbx / (kmsx * 1e-3) / 1e9
+        secondary["c128_binary64"] = {"value": round(step_bytes / (ms_x * 1e-3) / 1e9, 1), "unit": "GB/s",
+                                      "ms_per_step": round(ms_x, 2), "dtype": "f64",
+                                      "roofline": {"achieved": round(achx, 1), "frac": round(achx / peak, 4),
+                                                   "avg_launch_ms": round(kmsx / max(nlx, 1), 3)},
+                                      "note": "IEEE binary64 gate arithmetic: FP64-issue bound on GB300"}
+        exact.close()
         s64 = DenseGB300(n, "c64")
-        for _ in range(2):
-            s64.apply(circ)
-            s64.flush()
-        s64.profile(True)
-        ext64 = torch.cuda.ExternalStream(s64.stream_handle())
-        torch.cuda.synchronize()
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(ext64)
-        for _ in range(args.steps):
-            s64.apply(circ)
-            s64.flush()
-        a1.record(ext64)
-        torch.cuda.synchronize()
-        ms64 = a0.elapsed_time(a1) / args.steps
-        nl64, kms64, kb64 = s64.profile_read()
+        ms64, nl64, kms64, kb64 = time_steps(s64, circ, args.steps, 2, torch)
         ach64 = kb64 / (kms64 * 1e-3) / 1e9
         secondary["c64"] = {"value": round(G * 2 * 8 * (1 << n) / (ms64 * 1e-3) / 1e9, 1), "unit": "GB/s",
                             "ms_per_step": round(ms64, 3), "sweeps_per_step": s64.last_flush_stats()[1],
+                            "dtype": "f32",
                             "roofline": {"achieved": round(ach64, 1), "frac": round(ach64 / peak, 4),
                                          "avg_launch_ms": round(kms64 / max(nl64, 1), 4)}}
         s64.close()
+    else:
+        sim.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -322,10 +351,12 @@ def run_ours(args, world, rank, local):
         line = {
             "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == "c128" else "f32",
+            "vs_baseline": None,
+            "dtype": "f32x2 (float-float, binary64 in HBM)" if fast else ("f64" if prec == "c128" else "f32"),
             "data": "synthetic: seeded random brickwork circuit (numpy default_rng(0))",
             "config": {"workload": "brickwork-%dq-%dlayers-%s" % (n, args.layers, prec), "qubits": n,
-                       "layers": args.layers, "gates": G, "precision": prec, "sweeps_per_step": passes,
+                       "layers": args.layers, "gates": G, "precision": prec,
+                       "arithmetic": "float-float" if fast else "native", "sweeps_per_step": passes,
                        "l2": "state %d GiB > 129 MB L2; no flush needed" % ((B << n) >> 30),
                        "parallelism": "replicas" if world > 1 else "single"},
             "sweep_gbs": round(world * passes * 2 * B * (1 << n) / (ms_step * 1e-3) / 1e9, 1),
@@ -345,6 +376,8 @@ def main():
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--prec", choices=["c64", "c128"], default="c128")
+    ap.add_argument("--arith", choices=["ff", "exact"], default="ff",
+                    help="complex128 gate arithmetic: float-float (default) or IEEE binary64")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

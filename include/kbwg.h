@@ -201,6 +201,10 @@ int32_t kbwg_profile_read(kbwg_sim *sim, uint64_t *launches, double *total_ms, d
 /* Bytes this library copied host->device and device->host (all handles). */
 int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h);
 
+/* ||a - b|| / ||b|| over two handles of equal size and precision (FP64
+ * reduction on a's device; both handles must live on the same device). */
+int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative);
+
 /* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
 int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
 

@@ -69,6 +69,7 @@ SIGNATURES = {
     "kbwg_profile": (_I32, [_P, _I32]),
     "kbwg_profile_read": (_I32, [_P, _U64P, _DP, _DP]),
     "kbwg_transfer_bytes": (_I32, [_U64P, _U64P]),
+    "kbwg_state_distance": (_I32, [_P, _P, _DP]),
     "kbwg_masked_norm_noalloc": (_I32, [_P, _U, _I32, ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "kbwg_last_error": (ctypes.c_char_p, []),
     "kbwg_launch_count": (ctypes.c_uint64, []),

@@ -758,6 +758,26 @@ int32_t kbwg_profile_read(kbwg_sim *s, uint64_t *launches, double *total_ms, dou
     GUARD_END
 }
 
+int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative) {
+    GUARD_BEGIN
+    if (!a || !b || !relative) return fail(KBWG_EINVAL, "null argument");
+    if (a->n != b->n || a->prec != b->prec || a->device != b->device)
+        return fail(KBWG_EINVAL, "handles differ in size, precision or device");
+    ENTER(a);
+    CUDA_TRY(flush_queue(*a));
+    CUDA_TRY(flush_queue(*b));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(dispatch(a, [&](auto *tp) {
+        using T = std::remove_pointer_t<decltype(tp)>;
+        return launch_distance<T>(a->state, b->state, a->n, a->rs, a->stream);
+    }));
+    CUDA_TRY(copy_async(a->h_result, a->rs.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, a->stream));
+    CUDA_TRY(cudaStreamSynchronize(a->stream));
+    *relative = a->h_result[1] > 0 ? sqrt(a->h_result[0] / a->h_result[1]) : sqrt(a->h_result[0]);
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h) {
     if (h2d) *h2d = g_h2d_bytes.load();
     if (d2h) *d2h = g_d2h_bytes.load();

@@ -39,6 +39,9 @@ struct GateDesc {
 };
 
 enum { G_X = 0, G_Y = 1, G_Z = 2, G_H = 3, G_P = 4, G_RX = 5, G_RY = 6, G_RZ = 7 };
+// Internal kinds of the complex128 float-float path (never seen at the ABI):
+// H without its 1/sqrt(2), |1> times i^q (c[0] = q), multiply every amplitude by c[0] + i c[1].
+enum { G_HN = 8, G_PI = 9, G_SCALE = 10 };
 
 #if defined(__CUDACC__)
 // ---- rounding-exact arithmetic -------------------------------------------
@@ -160,7 +163,7 @@ __device__ __forceinline__ void apply_pair(uint32_t kind, const GateK<T> &k, cx<
 
 // Diagonal gates: each amplitude only picks up a phase.
 __host__ __device__ __forceinline__ bool is_diag_kind(uint32_t kind) {
-    return kind == G_Z || kind == G_P || kind == G_RZ;
+    return kind == G_Z || kind == G_P || kind == G_RZ || kind == G_PI || kind == G_SCALE;
 }
 
 // Gates that only change the |1> amplitude of the pair.

@@ -41,6 +41,10 @@ template <class T>
 cudaError_t launch_masked_norm(const void *st, uint32_t n, uint64_t M, uint64_t V, const ReduceScratch &rs,
                                cudaStream_t s);
 
+// sum |a - b|^2 into scratch.result[0] and sum |b|^2 into result[1].
+template <class T>
+cudaError_t launch_distance(const void *a, const void *b, uint32_t n, const ReduceScratch &rs, cudaStream_t s);
+
 // One step of the sequential measurement: conditional p1 of ctl->qubit[step]
 // given the outcomes so far, then the WeightedIndex decision, all on device.
 template <class T>

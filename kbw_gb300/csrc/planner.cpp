@@ -7,7 +7,7 @@
 
 namespace kbwg {
 
-bool is_diagonal(uint32_t kind) { return kind == G_Z || kind == G_P || kind == G_RZ; }
+bool is_diagonal(uint32_t kind) { return is_diag_kind(kind); }
 
 static inline uint64_t qubits_of(const GateDesc &g) { return g.ctrl | (1ull << g.target); }
 
@@ -57,7 +57,7 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
             const size_t i = remaining[ii];
             const GateDesc &x = g[i];
             const uint64_t qs = qubits_of(x);
-            bool ok = !(qs & blocked);
+            bool ok = !(qs & blocked) && take.size() < (size_t)kMaxSweepGates;
             if (ok && !is_diagonal(x.kind) && x.target >= (uint32_t)kLaneBits) {
                 const uint64_t b = 1ull << x.target;
                 if (!(needed & b)) {
@@ -128,14 +128,26 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                 const GateDesc &x = g[i];
                 TileGate t;
                 memset(&t, 0, sizeof t);
-                t.kind = x.kind;
+                switch (x.kind) {
+                case G_X: t.cls = TG_PERM; t.sub = 0; break;
+                case G_Y: t.cls = TG_PERM; t.sub = 1; break;
+                case G_H: t.cls = TG_H; break;
+                case G_RY: t.cls = TG_ROT; t.sub = 0; break;
+                case G_RX: t.cls = TG_ROT; t.sub = 1; break;
+                case G_Z: t.cls = TG_DIAG; t.sub = 0; break;
+                case G_P: t.cls = TG_DIAG; t.sub = 1; break;
+                case G_RZ: t.cls = TG_DIAG; t.sub = 2; break;
+                case G_HN: t.cls = TG_H; t.sub = 1; break;
+                case G_PI: t.cls = TG_DIAG; t.sub = 3; break;
+                default: t.cls = TG_DIAG; t.sub = 5; break;  // G_SCALE
+                }
                 memcpy(t.c, x.c, sizeof t.c);
                 const int lb = local_bit(sw, x.target);
                 if (lb < 0) {  // diagonal gate on a qubit outside the tile
-                    t.flags = TG_OUTER_TARGET;
-                    t.tout = 1ull << x.target;
+                    t.tb = TG_OUTER;
+                    t.tout = (uint8_t)x.target;
                 } else {
-                    t.tb = (uint32_t)lb;
+                    t.tb = (uint8_t)lb;
                 }
                 uint64_t cm = x.ctrl;
                 while (cm) {

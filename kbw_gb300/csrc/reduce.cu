@@ -202,6 +202,47 @@ cudaError_t launch_masked_norm(const void *st, uint32_t n, uint64_t M, uint64_t 
     return cudaGetLastError();
 }
 
+// ---- distance between two states ----------------------------------------------
+// partials: sum |a - b|^2 and sum |b|^2 (two values per block).
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads)
+    k_distance(const cx<T> *__restrict__ a, const cx<T> *__restrict__ b, uint64_t count, ReduceScratch rs) {
+    typename AccOf<T>::type d, nb;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const cx<T> x = a[i], y = b[i];
+        const T dr = x.re - y.re, di = x.im - y.im;
+        d.add_prod(dr, dr);
+        d.add_prod(di, di);
+        nb.add_prod(y.re, y.re);
+        nb.add_prod(y.im, y.im);
+    }
+    const double vd = block_sum(d.value());
+    const double vn = block_sum(nb.value());
+    if (threadIdx.x == 0) {
+        rs.partials[2 * blockIdx.x] = vd;
+        rs.partials[2 * blockIdx.x + 1] = vn;
+    }
+    if (last_block(rs.ticket)) {
+        const double td = sum_partials(rs.partials, gridDim.x, 2, 0);
+        const double tn = sum_partials(rs.partials, gridDim.x, 2, 1);
+        if (threadIdx.x == 0) {
+            rs.result[0] = td;
+            rs.result[1] = tn;
+            *rs.ticket = 0;
+        }
+    }
+}
+
+template <class T>
+cudaError_t launch_distance(const void *a, const void *b, uint32_t n, const ReduceScratch &rs, cudaStream_t s) {
+    k_distance<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)a, (const cx<T> *)b, 1ull << n, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+template cudaError_t launch_distance<float>(const void *, const void *, uint32_t, const ReduceScratch &, cudaStream_t);
+template cudaError_t launch_distance<double>(const void *, const void *, uint32_t, const ReduceScratch &, cudaStream_t);
+
 // ---- sequential measurement step ------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kReduceThreads)

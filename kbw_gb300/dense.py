@@ -217,6 +217,12 @@ class DenseGB300:
         N.check(self._lib.kbwg_profile_read(self._h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
         return int(n.value), float(ms.value), float(b.value)
 
+    def distance(self, other):
+        """||self - other|| / ||other||, computed on the device."""
+        out = ctypes.c_double()
+        N.check(self._lib.kbwg_state_distance(self._h, other._h, ctypes.byref(out)))
+        return out.value
+
     def last_flush_stats(self):
         g = ctypes.c_uint64()
         p = ctypes.c_uint64()

@@ -288,3 +288,49 @@ def test_28q_brickwork_round_trip(prec):
     st, re, im = sim.dump(list(range(n)))
     tol = 1e-12 if prec == "c128" else 1e-4
     assert st[0] == 0 and abs(re[0] - 1.0) < tol
+
+
+# ---- complex128 float-float fast path ------------------------------------------
+
+@pytest.mark.parametrize("n,gates,seed", [(12, 300, 61), (16, 500, 62), (20, 800, 63), (23, 400, 64)])
+def test_fast_c128_random_circuits(n, gates, seed):
+    """Float-float arithmetic on binary64 storage: amplitudes within 1e-12
+    relative of the restated Dense<f64>."""
+    circ = C.random_circuit(n, gates, seed, max_controls=3)
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, "c128")
+    ref.apply(circ)
+    assert rel_err(sim.state(), ref.state()) < 1e-12
+
+
+def test_fast_c128_brickwork_and_readout():
+    n = 20
+    circ = C.brickwork(n, 20, 0)
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, "c128")
+    ref.apply(circ)
+    assert rel_err(sim.state(), ref.state()) < 1e-12
+    zs = [(1.0, [(C.PAULI_Z, q)]) for q in range(n)]
+    assert abs(sim.exp_value(zs) - ref.exp_value(zs)) < 1e-11
+    for t in (0, 7, 19):
+        assert abs(sim.measure_p1(t) - ref.measure_p1(t)) < 1e-12
+    draws = C.uniform_draws(n, 3)
+    assert sim.measure(list(range(n)), draws) == ref.measure(list(range(n)), draws)
+
+
+def test_fast_c128_many_hadamards_rescale():
+    """More than 100 uncontrolled H in one flush forces an intermediate
+    rescale of the folded 1/sqrt(2) factors."""
+    n = 14
+    circ = []
+    for layer in range(30):
+        circ += [(C.H, q, (), 0.0) for q in range(n)]
+        circ += [(C.RZ, q, (), 0.3 * q + layer) for q in range(n)]
+        circ += [(C.X, (q + 1) % n, (q,), 0.0) for q in range(0, n - 1, 2)]
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, "c128")
+    ref.apply(circ)
+    assert rel_err(sim.state(), ref.state()) < 1e-12
