@@ -216,6 +216,48 @@ def time_steps(sim, circ, steps, warmup, torch):
     return e0.elapsed_time(e1) / steps, nl, kms, kbytes
 
 
+def run_adjoint_bench(args, torch, DenseGB300, C):
+    """Gradient half of the metric: 24 qubits, 10 layers of RY, RZ on every
+    qubit + CZ ring (480 parameters), ring TFIM.  grads/s of the adjoint
+    kernel vs the parameter-shift rule on the same GPU, plus the max
+    gradient error of each precision against the binary64 adjoint."""
+    n, L = args.adj_qubits, args.adj_layers
+    params = C.hea_params(n, L, 0)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    npar = len(params)
+    out = {"config": "hea-%dq-%dlayers-%dparams-tfim-ring" % (n, L, npar)}
+    ref_g = None
+    # binary64 first: its gradient is the reference for the error columns
+    for label, prec, fast in (("c128_binary64", "c128", False), ("c64", "c64", False), ("c128_ff", "c128", True)):
+        sim = DenseGB300(n, prec, fast_c128=fast)
+        sim.adjoint_gradient(circ, pidx, npar, ham)  # warm-up
+        torch.cuda.synchronize()
+        reps = 1 if label == "c128_binary64" else args.adj_reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e, g = sim.adjoint_gradient(circ, pidx, npar, ham)
+        torch.cuda.synchronize()
+        ta = (time.perf_counter() - t0) / reps
+        item = {"energy": e, "adjoint_s": round(ta, 5), "adjoint_grads_per_s": round(npar / ta, 1)}
+        if ref_g is None:
+            ref_g = g
+        else:
+            item["max_grad_err_vs_binary64_adjoint"] = float(np.max(np.abs(g - ref_g)))
+        if label == "c64" or (label == "c128_ff" and args.adj_ps_c128):
+            t0 = time.perf_counter()
+            e_ps, g_ps = sim.param_shift_gradient(circ, pidx, npar, ham)
+            torch.cuda.synchronize()
+            tp = time.perf_counter() - t0
+            item.update({"param_shift_s": round(tp, 4), "param_shift_grads_per_s": round(npar / tp, 2),
+                         "speedup_adjoint_vs_param_shift": round(tp / ta, 1),
+                         "max_grad_err_vs_param_shift": float(np.max(np.abs(g - g_ps)))})
+        out[label] = item
+        sim.close()
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import kbw_gb300
@@ -339,6 +381,9 @@ def run_ours(args, world, rank, local):
     else:
         sim.close()
 
+    if args.adjoint:
+        secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, info = cpu_port_rate(n, prec, circ, args.cpu_seconds)
@@ -383,6 +428,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-gates", type=int, default=4)
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
+    ap.add_argument("--adj-qubits", type=int, default=24)
+    ap.add_argument("--adj-layers", type=int, default=10)
+    ap.add_argument("--adj-reps", type=int, default=3)
+    ap.add_argument("--adj-ps-c128", action="store_true", help="also time parameter shift in float-float complex128")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per sweep launch, when known")
     args = ap.parse_args()

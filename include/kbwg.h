@@ -151,6 +151,35 @@ int32_t kbwg_exp_value(kbwg_sim *sim, const uint8_t *paulis, const uintptr_t *qu
                        const uintptr_t *offsets, const double *coefficients, uintptr_t n_strings,
                        double *out);
 
+/* Gradient of E = <psi|H|psi>, psi = gates|0...0>, by the reverse-mode
+ * adjoint method: forward, lambda = H psi, then one backward walk that
+ * uncomputes both states with inverse gates and accumulates
+ * dE/dtheta = Im<lambda|Pi_C P|phi> per RX/RY/RZ (P = X/Y/Z of the target,
+ * Pi_C the control projector) and -2 Im<lambda|Pi_C Pi_1|phi> per phase gate.
+ * Replaces the parameter-shift rule libket runs when the backend reports no
+ * native gradient (BatchExecution::gradient, src/quantum_execution.rs:420-426;
+ * GradientStrategy::ParameterShiftRule, :237-241).
+ * param_index[i] in [0, n_params) marks gate i (P/RX/RY/RZ only) as depending
+ * on parameter param_index[i] (shared parameters add up); -1 = constant.  The
+ * Hamiltonian is given as in kbwg_exp_value.  Up to max_checkpoints copies of
+ * the forward state (as memory allows) bound the uncompute drift.  Writes E
+ * and gradient[n_params]; the handle is left in |0...0>.  Needs >= 12 qubits
+ * (complex64) or >= 11 (complex128). */
+int32_t kbwg_adjoint_gradient(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates,
+                              const int32_t *param_index, uintptr_t n_params, const uint8_t *paulis,
+                              const uintptr_t *qubits, const uintptr_t *offsets, const double *coefficients,
+                              uintptr_t n_strings, uint32_t max_checkpoints, double *energy, double *gradient);
+
+/* The same gradient by the parameter-shift rule on the GPU, the strategy
+ * libket applies to KBW (GradientStrategy::ParameterShiftRule,
+ * src/quantum_execution.rs:237-241): two fresh circuit evaluations
+ * (BatchExecution::exp_value, :392-405) per parameterised gate, at
+ * theta +- pi/2.  The handle is left in the last evaluated state. */
+int32_t kbwg_param_shift_gradient(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates,
+                                  const int32_t *param_index, uintptr_t n_params, const uint8_t *paulis,
+                                  const uintptr_t *qubits, const uintptr_t *offsets, const double *coefficients,
+                                  uintptr_t n_strings, double *energy, double *gradient);
+
 /* QuantumExecution::clear (src/quantum_execution.rs:161; src/dense.rs:399-406). */
 int32_t kbwg_clear(kbwg_sim *sim);
 

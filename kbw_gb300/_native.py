@@ -54,6 +54,10 @@ SIGNATURES = {
     "kbwg_dump": (_I32, [_P, _UP, _U, _U64P, _DP, _DP, _U, _UP]),
     "kbwg_sample": (_I32, [_P, _UP, _U, _U, _DP, _U64P, _U64P, _U, _UP]),
     "kbwg_exp_value": (_I32, [_P, ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, _DP]),
+    "kbwg_adjoint_gradient": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_int32), _U,
+                                     ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, ctypes.c_uint32, _DP, _DP]),
+    "kbwg_param_shift_gradient": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_int32), _U,
+                                         ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, _DP, _DP]),
     "kbwg_clear": (_I32, [_P]),
     "kbwg_flush": (_I32, [_P]),
     "kbwg_get_state": (_I32, [_P, _P, _U]),

@@ -110,6 +110,20 @@ def hea(num_qubits, layers, params):
     return g
 
 
+def hea_param_index(num_qubits, layers):
+    """param_index of hea(): each RY/RZ has its own parameter, CZ gates none."""
+    n = num_qubits
+    idx = []
+    k = 0
+    for _ in range(layers):
+        for _q in range(2 * n):
+            idx.append(k)
+            k += 1
+        if n >= 2:
+            idx += [-1] * (n if n > 2 else 1)
+    return idx
+
+
 def hea_params(num_qubits, layers, seed):
     return np.random.default_rng(seed).uniform(-math.pi, math.pi, size=2 * num_qubits * layers)
 

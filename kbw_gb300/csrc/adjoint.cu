@@ -1,0 +1,707 @@
+// Reverse-mode adjoint gradient of E(theta) = <psi|H|psi>, psi = U_M...U_1|0>.
+//
+// The reference has no native gradient: BatchExecution::gradient returns
+// NativeGateUnsupported (kbw src/quantum_execution.rs:420-426) and libket
+// falls back to the parameter-shift rule, two full circuit evaluations per
+// parameter (src/quantum_execution.rs:237-241, 392-405).  Here:
+//   1. forward: phi = psi with the fused sweeps, copying phi at segment
+//      boundaries ("checkpoints") while memory allows;
+//   2. lambda = H phi (one pass per group of Pauli strings sharing X/Y
+//      positions), E = Re<phi|lambda>;
+//   3. reverse: walk the gates backwards; for gate j (phi = phi_j,
+//      lambda = lambda_j) accumulate
+//        RX/RY/RZ(t) = exp(-i t P/2):  dE/dt = Im <lambda| Pi_C P |phi>
+//        P(t) = diag(1, e^{it}):       dE/dt = -2 Im <lambda| Pi_C Pi_1 |phi>
+//      (Pi_C = projector on the gate's controls), then uncompute
+//      phi <- U_j^dag phi and lambda <- U_j^dag lambda.  Both states move
+//      through one fused two-state tile sweep; at a checkpoint boundary phi
+//      is reloaded from its copy so rounding does not accumulate across
+//      segments.
+// Inner products accumulate FP64-grade (float partials per warp widened to
+// double for complex64, double or float-float for complex128).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/kbwg.h"
+#include "kernels.h"
+#include "sim.h"
+#include "sweep_dev.cuh"
+
+namespace kbwg {
+
+// ---- lambda = H phi ------------------------------------------------------------------
+// One group of strings with common flip mask x:
+//   lambda_s (+)= sum_k c_k i^{ny_k} (-1)^{|(s^x) & z_k|} phi_{s^x}
+struct ApplyGroup {
+    uint64_t x;
+    uint32_t nterms;
+    uint32_t init;  // 1: write lambda instead of accumulating
+    uint64_t z[kMaxTerms];
+    double cre[kMaxTerms];  // c_k * Re(i^{ny_k})
+    double cim[kMaxTerms];  // c_k * Im(i^{ny_k})
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) k_apply_group(const cx<T> *__restrict__ phi, cx<T> *__restrict__ lam,
+                                                     uint64_t ns, ApplyGroup g) {
+    __shared__ T sre[kMaxTerms], sim_[kMaxTerms];
+    if (threadIdx.x < kMaxTerms) {
+        sre[threadIdx.x] = (T)g.cre[threadIdx.x];
+        sim_[threadIdx.x] = (T)g.cim[threadIdx.x];
+    }
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        const uint64_t src = s ^ g.x;
+        const cx<T> a = phi[src];
+        T wr = 0, wi = 0;
+        for (uint32_t k = 0; k < g.nterms; k++) {
+            const bool neg = (__popcll(src & g.z[k]) & 1) != 0;
+            wr += neg ? -sre[k] : sre[k];
+            wi += neg ? -sim_[k] : sim_[k];
+        }
+        cx<T> r;
+        r.re = wr * a.re - wi * a.im;
+        r.im = wr * a.im + wi * a.re;
+        if (!g.init) {
+            const cx<T> o = lam[s];
+            r.re += o.re;
+            r.im += o.im;
+        }
+        lam[s] = r;
+    }
+}
+
+// Re<a|b> (FP64-grade) into result[0].
+template <class T>
+__global__ void __launch_bounds__(256) k_inner_re(const cx<T> *__restrict__ a, const cx<T> *__restrict__ b,
+                                                  uint64_t ns, double *partials, unsigned *ticket, double *result) {
+    double acc = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        const cx<T> x = a[s], y = b[s];
+        acc = fma((double)x.re, (double)y.re, acc);
+        acc = fma((double)x.im, (double)y.im, acc);
+    }
+    __shared__ double sh[8];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+        partials[blockIdx.x] = t;
+        __threadfence();
+        if (atomicAdd(ticket, 1u) == gridDim.x - 1) {
+            double tot = 0.0;
+            for (unsigned b2 = 0; b2 < gridDim.x; b2++) tot += partials[b2];
+            result[0] = tot;
+            *ticket = 0;
+        }
+    }
+}
+
+// ---- gradient terms --------------------------------------------------------------------
+// Contribution of one amplitude (lam, phi) whose pair partner is phip, on
+// the |one> side of the target bit:
+//   X: Im(conj(lam) phip)          Y: (one ? +1 : -1) Re(conj(lam) phip)
+//   Z: (one ? -1 : +1) Im(conj(lam) phi)     P1: one ? -2 Im(conj(lam) phi) : 0
+template <class P> struct Grad;
+
+template <class T>
+struct Grad<Exact<T>> {
+    using Amp = cx<T>;
+    using Acc = T;
+    static __device__ __forceinline__ Acc zero() { return (T)0; }
+    static __device__ __forceinline__ Acc term(int gt, bool one, Amp l, Amp p, Amp pp) {
+        switch (gt) {
+        case GT_X: return l.re * pp.im - l.im * pp.re;
+        case GT_Y: {
+            const T r = l.re * pp.re + l.im * pp.im;
+            return one ? r : -r;
+        }
+        case GT_Z: {
+            const T r = l.re * p.im - l.im * p.re;
+            return one ? -r : r;
+        }
+        default: return one ? (T)-2 * (l.re * p.im - l.im * p.re) : (T)0;
+        }
+    }
+    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
+    static __device__ __forceinline__ double warp_total(Acc a) {
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        return (double)a;
+    }
+};
+
+template <>
+struct Grad<FFPol> {
+    using Amp = FFPol::Amp;
+    using Acc = ff::f2;
+    static __device__ __forceinline__ Acc zero() { return ff::f2{0.f, 0.f}; }
+    static __device__ __forceinline__ ff::f2 im_conj(const Amp &l, const Amp &b) {  // Im(conj(l) b)
+        return ff::dot2(l.re, b.im, ff::neg(l.im), b.re);
+    }
+    static __device__ __forceinline__ ff::f2 re_conj(const Amp &l, const Amp &b) {  // Re(conj(l) b)
+        return ff::dot2(l.re, b.re, l.im, b.im);
+    }
+    static __device__ __forceinline__ Acc term(int gt, bool one, const Amp &l, const Amp &p, const Amp &pp) {
+        switch (gt) {
+        case GT_X: return im_conj(l, pp);
+        case GT_Y: {
+            const ff::f2 r = re_conj(l, pp);
+            return one ? r : ff::neg(r);
+        }
+        case GT_Z: {
+            const ff::f2 r = im_conj(l, p);
+            return one ? ff::neg(r) : r;
+        }
+        default: {
+            if (!one) return zero();
+            const ff::f2 r = im_conj(l, p);
+            return ff::f2{-2.f * r.h, -2.f * r.l};
+        }
+        }
+    }
+    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return ff::add(a, b); }
+    static __device__ __forceinline__ double warp_total(Acc a) {
+        for (int o = 16; o > 0; o >>= 1) {
+            Acc b{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+            a = ff::add(a, b);
+        }
+        return (double)a.h + (double)a.l;
+    }
+};
+
+template <class P, int R, int B>
+__device__ __forceinline__ typename Grad<P>::Acc grad_pairs(int gt, const typename P::Amp (&ph)[1 << R],
+                                                           const typename P::Amp (&la)[1 << R], uint32_t creg) {
+    using G = Grad<P>;
+    typename G::Acc acc = G::zero();
+#pragma unroll
+    for (int jj = 0; jj < (1 << (R - 1)); jj++) {
+        const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
+        const int j1 = j0 | (1 << B);
+        if (creg == 0u || ((uint32_t)j0 & creg) == creg) {
+            acc = G::add(acc, G::term(gt, false, la[j0], ph[j0], ph[j1]));
+            acc = G::add(acc, G::term(gt, true, la[j1], ph[j1], ph[j0]));
+        }
+    }
+    return acc;
+}
+
+// This thread's part of the gradient inner product of one step.  Every lane
+// must call it (lane-bit targets shuffle).
+template <class P, int K, int R>
+__device__ __forceinline__ typename Grad<P>::Acc grad_partial(const TileGate &g, int gt,
+                                                             const typename P::Amp (&ph)[1 << R],
+                                                             const typename P::Amp (&la)[1 << R], int R0,
+                                                             uint32_t F, uint64_t base) {
+    using G = Grad<P>;
+    constexpr int NR = 1 << R;
+    typename G::Acc acc = G::zero();
+    const uint32_t regmask = (uint32_t)(NR - 1) << R0;
+    const uint32_t fixed_need = g.cl & ~regmask;
+    const bool fok = (F & fixed_need) == fixed_need;
+    const uint32_t creg = (g.cl & regmask) >> R0;
+    const uint32_t tb = g.tb;
+    if (gt == GT_Z || gt == GT_P1) {
+        if (!fok) return acc;
+        const int rb = (int)tb - R0;
+        if (tb != TG_OUTER && rb >= 0 && rb < R) {
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if (creg == 0u || ((uint32_t)j & creg) == creg)
+                    acc = G::add(acc, G::term(gt, ((j >> rb) & 1) != 0, la[j], ph[j], ph[j]));
+        } else {
+            const bool one = (tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0) : (((F >> tb) & 1u) != 0);
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if (creg == 0u || ((uint32_t)j & creg) == creg) acc = G::add(acc, G::term(gt, one, la[j], ph[j], ph[j]));
+        }
+        return acc;
+    }
+    if (tb < (uint32_t)kLaneBits) {
+        const bool one = ((F >> tb) & 1u) != 0;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp pp = P::shfl(ph[j], 1 << tb);
+            if (fok && (creg == 0u || ((uint32_t)j & creg) == creg)) acc = G::add(acc, G::term(gt, one, la[j], ph[j], pp));
+        }
+        return acc;
+    }
+    if (!fok) return acc;
+    switch ((int)tb - R0) {
+    case 0: return grad_pairs<P, R, 0>(gt, ph, la, creg);
+    case 1: return grad_pairs<P, R, 1>(gt, ph, la, creg);
+    case 2: return grad_pairs<P, R, 2>(gt, ph, la, creg);
+    default:
+        if constexpr (R > 3) return grad_pairs<P, R, (R > 3 ? 3 : 0)>(gt, ph, la, creg);
+        return acc;
+    }
+}
+
+// ---- two-state adjoint sweep -------------------------------------------------------------
+template <class T> struct AdjCfg;
+template <> struct AdjCfg<float> {
+    static constexpr int K = 12, R = 4;
+};
+template <> struct AdjCfg<double> {
+    static constexpr int K = 11, R = 3;
+};
+
+struct AdjParams {
+    SweepParams sw;
+    const uint32_t *ginfo;  // per program gate: gradient type | (slot << 4)
+    double *partials;       // [gridDim.x][nslots]
+    uint32_t nslots;
+};
+
+template <class P, int K, int R>
+struct AdjKernel {
+    using Mem = typename P::Mem;
+    static constexpr int kThreads = 32 << (K - kLaneBits - R);
+    static constexpr int kWarps = kThreads / 32;
+    static constexpr size_t kTileBytes = sizeof(Mem) << K;
+    static constexpr size_t kSmem = 2 * kTileBytes + 256 * sizeof(uint64_t) + kMaxSweepGates * sizeof(TileGate) +
+                                    kMaxSweepGates * sizeof(uint32_t) + (size_t)kWarps * kMaxSweepGates * sizeof(double) +
+                                    16;
+};
+
+template <class P, int K, int R>
+__global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads)
+    k_adjoint(typename P::Mem *__restrict__ phi, typename P::Mem *__restrict__ lam, const __grid_constant__ AdjParams a) {
+    using Amp = typename P::Amp;
+    using Mem = typename P::Mem;
+    using AK = AdjKernel<P, K, R>;
+    using G = Grad<P>;
+    constexpr int NR = 1 << R;
+    const SweepParams &p = a.sw;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Mem *tphi_m = reinterpret_cast<Mem *>(smem_raw);
+    Mem *tlam_m = reinterpret_cast<Mem *>(smem_raw + AK::kTileBytes);
+    Amp *tphi = reinterpret_cast<Amp *>(smem_raw);
+    Amp *tlam = reinterpret_cast<Amp *>(smem_raw + AK::kTileBytes);
+    unsigned char *q = smem_raw + 2 * AK::kTileBytes;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(q);
+    q += 256 * sizeof(uint64_t);
+    TileGate *sg = reinterpret_cast<TileGate *>(q);
+    q += kMaxSweepGates * sizeof(TileGate);
+    uint32_t *sinfo = reinterpret_cast<uint32_t *>(q);
+    q += kMaxSweepGates * sizeof(uint32_t);
+    double *acc = reinterpret_cast<double *>(q);  // [kWarps][kMaxSweepGates]
+    q += (size_t)AK::kWarps * kMaxSweepGates * sizeof(double);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(q);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t l = p.l, m = p.m;
+    const uint32_t chunk = 1u << l, nchunks = 1u << m;
+    const uint32_t chunk_bytes = chunk * (uint32_t)sizeof(Mem);
+    const uint64_t lowmask = chunk - 1;
+
+    for (uint32_t i = threadIdx.x; i < p.gate_count; i += blockDim.x) {
+        sg[i] = p.prog[i];
+        sinfo[i] = a.ginfo[i];
+    }
+    for (uint32_t i = threadIdx.x; i < (uint32_t)AK::kWarps * kMaxSweepGates; i += blockDim.x) acc[i] = 0.0;
+    for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
+        chunk_off[c] = off;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto tile_base = [&](uint64_t tau) {
+        uint64_t b = tau << l;
+        for (uint32_t j = 0; j < m; j++) b = insert_zero_at(b, p.hq[j]);
+        return b;
+    };
+    auto issue_load = [&](uint64_t tau) {
+        if (warp == 0) {
+            const uint64_t b = tile_base(tau);
+            if (lane == 0) mbar_expect_tx(bar, (uint32_t)(2 * AK::kTileBytes));
+            __syncwarp();
+            for (uint32_t c = lane; c < nchunks; c += 32) {
+                tma_load(tphi_m + (size_t)c * chunk, phi + b + chunk_off[c], chunk_bytes, bar);
+                tma_load(tlam_m + (size_t)c * chunk, lam + b + chunk_off[c], chunk_bytes, bar);
+            }
+        }
+    };
+
+    uint64_t tau = blockIdx.x;
+    if (tau < p.tiles) issue_load(tau);
+    const uint32_t FA = (uint32_t)lane | ((uint32_t)warp << (kLaneBits + R));
+    const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
+    for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
+        const uint64_t base = tile_base(tau);
+        bool ok = false;
+        for (uint32_t spin = 0; spin < (1u << 22); spin++)
+            if (mbar_try_wait(bar, it & 1u)) {
+                ok = true;
+                break;
+            }
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(p.err, 1);
+            return;
+        }
+        Amp vp[NR], vl[NR];
+        int layout = p.stage_layout[0];
+        int R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
+        uint32_t F = (layout == LAYOUT_A) ? FA : FB;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            vp[j] = P::from_mem(tphi_m[F | ((uint32_t)j << R0)]);
+            vl[j] = P::from_mem(tlam_m[F | ((uint32_t)j << R0)]);
+        }
+        uint32_t g0 = 0;
+        for (uint32_t s = 0; s < p.nstages; s++) {
+            const int nl = p.stage_layout[s];
+            if (nl != layout) {
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    tphi[F | ((uint32_t)j << R0)] = vp[j];
+                    tlam[F | ((uint32_t)j << R0)] = vl[j];
+                }
+                __syncthreads();
+                layout = nl;
+                R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
+                F = (layout == LAYOUT_A) ? FA : FB;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    vp[j] = tphi[F | ((uint32_t)j << R0)];
+                    vl[j] = tlam[F | ((uint32_t)j << R0)];
+                }
+            }
+            const uint32_t g1 = p.stage_end[s];
+            for (uint32_t gi = g0; gi < g1; gi++) {
+                const TileGate &g = sg[gi];
+                if ((base & g.co) != g.co) continue;  // uniform over the tile
+                const uint32_t info = sinfo[gi];
+                const int gt = (int)(info & 15u);
+                if (gt != GT_NONE) {
+                    const double w = G::warp_total(grad_partial<P, K, R>(g, gt, vp, vl, R0, F, base));
+                    if (lane == 0) acc[warp * kMaxSweepGates + (info >> 4)] += w;
+                }
+                tile_gate<P, K, R>(g, vp, R0, F, base);
+                tile_gate<P, K, R>(g, vl, R0, F, base);
+            }
+            g0 = g1;
+        }
+        fence_proxy_async();
+        __syncthreads();
+        const uint64_t next = tau + gridDim.x;
+        if (next < p.tiles) issue_load(next);
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const uint32_t u = F | ((uint32_t)j << R0);
+            const uint64_t idx = base + chunk_off[u >> l] + (u & lowmask);
+            phi[idx] = P::to_mem(vp[j]);
+            lam[idx] = P::to_mem(vl[j]);
+        }
+    }
+    __syncthreads();
+    for (uint32_t sl = threadIdx.x; sl < a.nslots; sl += blockDim.x) {
+        double t = 0.0;
+        for (int w = 0; w < AK::kWarps; w++) t += acc[w * kMaxSweepGates + sl];
+        a.partials[(size_t)blockIdx.x * a.nslots + sl] = t;
+    }
+}
+
+// grads[gate_of_slot[s]] = sum over blocks of partials[b][s] (fixed order).
+__global__ void k_sum_slots(const double *partials, uint32_t nblocks, uint32_t nslots, const uint32_t *gate_of_slot,
+                            double *grads) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    double t = 0.0;
+    for (uint32_t b = 0; b < nblocks; b++) t += partials[(size_t)b * nslots + s];
+    grads[gate_of_slot[s]] = t;
+}
+
+// ---- host orchestration ----------------------------------------------------------------
+struct AdjBuffers {
+    void *lam = nullptr;
+    std::vector<void *> ckpt;
+    double *partials = nullptr;
+    double *grads = nullptr;
+    uint32_t *meta = nullptr;  // ginfo + gate_of_slot
+    void *prog = nullptr;
+    void release() {
+        if (lam) cudaFree(lam);
+        for (void *c : ckpt) cudaFree(c);
+        ckpt.clear();
+        if (partials) cudaFree(partials);
+        if (grads) cudaFree(grads);
+        if (meta) cudaFree(meta);
+        if (prog) cudaFree(prog);
+        lam = nullptr;
+        partials = grads = nullptr;
+        meta = nullptr;
+        prog = nullptr;
+    }
+};
+
+static GateDesc inverse_desc(int prec, const GateDesc &g, double angle) {
+    // X, Y, Z, H are their own inverses; P/RX/RY/RZ invert by negating the angle
+    switch (g.kind) {
+    case G_P:
+    case G_RX:
+    case G_RY:
+    case G_RZ: return make_gate_desc(prec, g.kind, g.target, g.ctrl, -angle);
+    default: return g;
+    }
+}
+
+template <class P, int K, int R>
+static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<GateDesc> &fwd,
+                                   const std::vector<double> &angles, const std::vector<int> &gtype, size_t lo,
+                                   size_t hi, int num_sms) {
+    using AK = AdjKernel<P, K, R>;
+    using Mem = typename P::Mem;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_adjoint<P, K, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AK::kSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    // reverse list of inverse gates; gradient info follows each gate through the planner
+    std::vector<GateDesc> rev;
+    std::vector<size_t> rev_src;
+    for (size_t j = hi; j-- > lo;) {
+        rev.push_back(inverse_desc(s.prec, fwd[j], angles[j]));
+        rev_src.push_back(j);
+    }
+    std::vector<PlannedSweep> plan = plan_sweeps(s.n, K, R, rev.data(), rev.size(), false);
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<P, K, R>, AK::kThreads, AK::kSmem);
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = 1ull << (s.n - K);
+    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * std::max(occ, 1));
+    for (const PlannedSweep &sw : plan) {
+        const size_t ng = sw.gates.size();
+        std::vector<TileGate> prog = sw.gates;
+        for (TileGate &t : prog) P::pack_host(t);
+        std::vector<uint32_t> meta(2 * kMaxSweepGates, 0);  // ginfo | gate_of_slot
+        uint32_t nslots = 0;
+        for (size_t i = 0; i < ng; i++) {
+            const size_t j = rev_src[sw.src[i]];
+            if (gtype[j] != GT_NONE) {
+                meta[i] = (uint32_t)gtype[j] | (nslots << 4);
+                meta[kMaxSweepGates + nslots] = (uint32_t)j;
+                nslots++;
+            }
+        }
+        e = copy_async(bufs.prog, prog.data(), ng * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
+        if (e != cudaSuccess) return e;
+        e = copy_async(bufs.meta, meta.data(), meta.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s.stream);
+        if (e != cudaSuccess) return e;
+        AdjParams a;
+        memset(&a, 0, sizeof a);
+        a.sw.hmask = sw.hmask;
+        a.sw.l = sw.l;
+        a.sw.m = sw.m;
+        memcpy(a.sw.hq, sw.hq, sizeof a.sw.hq);
+        a.sw.nstages = (uint32_t)sw.stage_layout.size();
+        a.sw.gate_count = (uint32_t)ng;
+        for (uint32_t i = 0; i < a.sw.nstages; i++) {
+            a.sw.stage_layout[i] = sw.stage_layout[i];
+            a.sw.stage_end[i] = sw.stage_end[i];
+        }
+        a.sw.prog = (const TileGate *)bufs.prog;
+        a.sw.err = s.d_err;
+        a.sw.tiles = tiles;
+        a.ginfo = bufs.meta;
+        a.partials = bufs.partials;
+        a.nslots = nslots;
+        if (s.prof.on) s.prof.mark(s.stream);
+        k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)bufs.lam, a);
+        count_launch();
+        e = cudaGetLastError();
+        if (s.prof.on) {
+            s.prof.mark(s.stream);
+            s.prof.bytes += 4.0 * (double)s.elem * (double)s.ns;
+        }
+        if (e != cudaSuccess) return e;
+        if (nslots) {
+            k_sum_slots<<<(nslots + 127) / 128, 128, 0, s.stream>>>(bufs.partials, (uint32_t)grid, nslots,
+                                                                    bufs.meta + kMaxSweepGates, bufs.grads);
+            count_launch();
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        // the program/meta buffers are reused by the next sweep: wait for this one
+        e = cudaStreamSynchronize(s.stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <class T>
+static cudaError_t apply_hamiltonian(Sim &s, void *lam, const std::vector<ApplyGroup> &groups) {
+    const uint64_t ns = s.ns;
+    uint64_t g = (ns + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    for (const ApplyGroup &ag : groups) {
+        k_apply_group<T><<<(unsigned)g, 256, 0, s.stream>>>((const cx<T> *)s.state, (cx<T> *)lam, ns, ag);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <class T>
+static cudaError_t inner_re(Sim &s, const void *a, const void *b, double *out) {
+    k_inner_re<T><<<kReduceBlocks, 256, 0, s.stream>>>((const cx<T> *)a, (const cx<T> *)b, s.ns, s.rs.partials,
+                                                        s.rs.ticket, s.rs.result);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = copy_async(s.h_result, s.rs.result, sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s.stream);
+    *out = s.h_result[0];
+    return e;
+}
+
+static std::vector<ApplyGroup> make_groups(const std::vector<PauliString> &H) {
+    std::vector<size_t> order(H.size());
+    for (size_t k = 0; k < H.size(); k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return H[a].x < H[b].x; });
+    std::vector<ApplyGroup> groups;
+    size_t i = 0;
+    while (i < order.size()) {
+        ApplyGroup g;
+        memset(&g, 0, sizeof g);
+        g.x = H[order[i]].x;
+        while (i < order.size() && H[order[i]].x == g.x && g.nterms < (uint32_t)kMaxTerms) {
+            const PauliString &t = H[order[i]];
+            const int k = (int)g.nterms++;
+            g.z[k] = t.z;
+            const int m = t.ny & 3;  // i^ny
+            g.cre[k] = (m == 0) ? t.coef : (m == 2 ? -t.coef : 0.0);
+            g.cim[k] = (m == 1) ? t.coef : (m == 3 ? -t.coef : 0.0);
+            i++;
+        }
+        g.init = groups.empty() ? 1u : 0u;
+        groups.push_back(g);
+    }
+    if (groups.empty()) {  // H = 0
+        ApplyGroup g;
+        memset(&g, 0, sizeof g);
+        g.init = 1;
+        groups.push_back(g);
+    }
+    return groups;
+}
+
+template <class P, class T, int K, int R>
+static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
+                           const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
+                           std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
+    AdjBuffers bufs;
+    auto fail_cuda = [&](cudaError_t e, const char *what) {
+        bufs.release();
+        cudaGetLastError();
+        set_error(e == cudaErrorMemoryAllocation ? KBWG_ENOMEM : KBWG_ECUDA,
+                  std::string("adjoint: ") + what + ": " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? (int32_t)KBWG_ENOMEM : (int32_t)KBWG_ECUDA;
+    };
+    const size_t M = fwd.size();
+    const size_t sb = (size_t)s.ns * s.elem;
+    int dev = 0, num_sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail_cuda(e, "device query");
+    e = cudaMalloc(&bufs.lam, sb);
+    if (e != cudaSuccess) return fail_cuda(e, "lambda buffer");
+    e = cudaMalloc((void **)&bufs.partials, (size_t)num_sms * 8 * kMaxSweepGates * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&bufs.grads, std::max<size_t>(M, 1) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&bufs.meta, 2 * kMaxSweepGates * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&bufs.prog, kMaxSweepGates * sizeof(TileGate));
+    if (e != cudaSuccess) return fail_cuda(e, "scratch");
+    // checkpoints: as many as fit in 80% of the free memory, at most max_ckpt
+    size_t free_b = 0, total_b = 0;
+    e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) return fail_cuda(e, "memory query");
+    size_t nck = std::min<size_t>(max_ckpt, (size_t)(0.8 * (double)free_b) / sb);
+    nck = std::min<size_t>(nck, M > 1 ? M - 1 : 0);
+    for (size_t i = 0; i < nck; i++) {
+        void *c = nullptr;
+        if (cudaMalloc(&c, sb) != cudaSuccess) {
+            cudaGetLastError();
+            break;
+        }
+        bufs.ckpt.push_back(c);
+    }
+    const size_t S = bufs.ckpt.size() + 1;
+    std::vector<size_t> b(S + 1);
+    for (size_t i = 0; i <= S; i++) b[i] = i * M / S;
+
+    // 1. forward from |0>
+    s.queue.clear();
+    e = launch_init<T>(s.state, s.n, s.stream);
+    if (e != cudaSuccess) return fail_cuda(e, "init");
+    for (size_t seg = 0; seg < S; seg++) {
+        s.queue.assign(fwd.begin() + b[seg], fwd.begin() + b[seg + 1]);
+        e = flush_queue(s);
+        if (e != cudaSuccess) return fail_cuda(e, "forward");
+        if (seg + 1 < S) {
+            e = cudaMemcpyAsync(bufs.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
+            if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
+        }
+    }
+    // 2. lambda = H phi, E = Re<phi|lambda>
+    e = apply_hamiltonian<T>(s, bufs.lam, make_groups(H));
+    if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
+    e = inner_re<T>(s, s.state, bufs.lam, energy);
+    if (e != cudaSuccess) return fail_cuda(e, "energy");
+    // 3. reverse, segment by segment
+    e = cudaMemsetAsync(bufs.grads, 0, std::max<size_t>(M, 1) * sizeof(double), s.stream);
+    if (e != cudaSuccess) return fail_cuda(e, "gradient buffer");
+    for (size_t seg = S; seg-- > 0;) {
+        e = adjoint_segment<P, K, R>(s, bufs, fwd, angles, gtype, b[seg], b[seg + 1], num_sms);
+        if (e != cudaSuccess) return fail_cuda(e, "reverse sweep");
+        if (seg > 0) {
+            e = cudaMemcpyAsync(s.state, bufs.ckpt[seg - 1], sb, cudaMemcpyDeviceToDevice, s.stream);
+            if (e != cudaSuccess) return fail_cuda(e, "checkpoint reload");
+        }
+    }
+    grad_per_gate.assign(M, 0.0);
+    if (M) {
+        e = copy_async(grad_per_gate.data(), bufs.grads, M * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+        if (e != cudaSuccess) return fail_cuda(e, "gradient read-back");
+    }
+    // leave the handle in |0...0>
+    e = launch_init<T>(s.state, s.n, s.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) return fail_cuda(e, "finish");
+    bufs.release();
+    return KBWG_OK;
+}
+
+int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
+                         const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
+                         std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
+    if (s.n < (uint32_t)AdjCfg<float>::K || (s.prec && s.n < (uint32_t)AdjCfg<double>::K)) {
+        set_error(KBWG_EUNSUPPORTED, "adjoint: needs at least 12 qubits (complex64) or 11 (complex128)");
+        return KBWG_EUNSUPPORTED;
+    }
+    if (s.prec == 0)
+        return adjoint_run<Exact<float>, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
+                                                                                  grad_per_gate, max_ckpt);
+    if (s.flags & KBWG_FLAG_FAST_C128)
+        return adjoint_run<FFPol, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
+                                                                             grad_per_gate, max_ckpt);
+    return adjoint_run<Exact<double>, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
+                                                                                 grad_per_gate, max_ckpt);
+}
+
+}  // namespace kbwg

@@ -541,23 +541,22 @@ int32_t kbwg_sample(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, ui
     GUARD_END
 }
 
-int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubits, const uintptr_t *offsets,
-                       const double *coefficients, uintptr_t n_strings, double *out) {
-    GUARD_BEGIN
-    ENTER(s);
-    if (!out || (n_strings && (!offsets || !coefficients))) return fail(KBWG_EINVAL, "null argument");
-    struct Str {
-        uint64_t x, z;
-        int ny;
-    };
-    std::vector<Str> strs(n_strings);
+}  // extern "C"
+
+// Parse the flattened Pauli strings of the ABI.  Returns 0 or KBWG_EINVAL.
+static int32_t parse_hamiltonian(uint32_t n, const uint8_t *paulis, const uintptr_t *qubits,
+                                 const uintptr_t *offsets, const double *coefficients, uintptr_t n_strings,
+                                 std::vector<PauliString> &out) {
+    if (n_strings && (!offsets || !coefficients)) return fail(KBWG_EINVAL, "null Hamiltonian arrays");
+    out.assign(n_strings, PauliString());
     for (uintptr_t k = 0; k < n_strings; k++) {
-        Str t{0, 0, 0};
+        PauliString t;
+        t.coef = coefficients[k];
         if (offsets[k + 1] < offsets[k]) return fail(KBWG_EINVAL, "offsets not ascending");
         for (uintptr_t i = offsets[k]; i < offsets[k + 1]; i++) {
             if (!paulis || !qubits) return fail(KBWG_EINVAL, "null term arrays");
             const uintptr_t q = qubits[i];
-            if (q >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
+            if (q >= n) return fail(KBWG_EINVAL, "qubit out of range");
             const uint64_t bit = 1ull << q;
             if ((t.x | t.z) & bit) return fail(KBWG_EINVAL, "qubit repeated in one Pauli string");
             switch (paulis[i]) {
@@ -567,13 +566,17 @@ int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubi
             default: return fail(KBWG_EINVAL, "bad Pauli code");
             }
         }
-        strs[k] = t;
+        out[k] = t;
     }
-    CUDA_TRY(flush_queue(*s));
-    // group strings by flip mask; per group launch in chunks of kMaxTerms
-    std::vector<uintptr_t> order(n_strings);
-    for (uintptr_t k = 0; k < n_strings; k++) order[k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](uintptr_t a, uintptr_t b) { return strs[a].x < strs[b].x; });
+    return KBWG_OK;
+}
+
+// <psi|H|psi> on the handle's current state (queue flushed by the caller).
+static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs, double *out) {
+    const size_t n_strings = strs.size();
+    std::vector<size_t> order(n_strings);
+    for (size_t k = 0; k < n_strings; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return strs[a].x < strs[b].x; });
     CUDA_TRY(s->tmp3.ensure((n_strings + 1) * 8));
     double *d_vals = (double *)s->tmp3.ptr;
     size_t i = 0;
@@ -581,9 +584,9 @@ int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubi
         PauliGroup g;
         memset(&g, 0, sizeof g);
         g.x = strs[order[i]].x;
-        std::vector<uintptr_t> idx;
+        std::vector<size_t> idx;
         while (i < n_strings && strs[order[i]].x == g.x && idx.size() < (size_t)kMaxTerms) {
-            const Str &t = strs[order[i]];
+            const PauliString &t = strs[order[i]];
             const int k = (int)idx.size();
             g.z[k] = t.z;
             if (g.x == 0) {
@@ -603,15 +606,137 @@ int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubi
             return launch_pauli_group<T>(s->state, s->n, g, s->rs, s->stream);
         }));
         for (size_t k = 0; k < idx.size(); k++)
-            CUDA_TRY(copy_async(d_vals + idx[k], s->rs.result + k, 8, cudaMemcpyDeviceToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(d_vals + idx[k], s->rs.result + k, 8, cudaMemcpyDeviceToDevice, s->stream));
     }
     std::vector<double> vals(n_strings + 1);
-    if (n_strings)
-        CUDA_TRY(copy_async(vals.data(), d_vals, n_strings * 8, cudaMemcpyDeviceToHost, s->stream));
+    if (n_strings) CUDA_TRY(copy_async(vals.data(), d_vals, n_strings * 8, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     double total = 0.0;  // sum in string order, as the reference's zip/map/sum
-    for (uintptr_t k = 0; k < n_strings; k++) total += vals[k] * coefficients[k];
+    for (size_t k = 0; k < n_strings; k++) total += vals[k] * strs[k].coef;
     *out = total;
+    return KBWG_OK;
+}
+
+// Validate a gradient circuit; fills the engine gates, angles and gradient types.
+static int32_t parse_grad_circuit(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates, const int32_t *param_index,
+                                  uintptr_t n_params, std::vector<GateDesc> &fwd, std::vector<double> &angles,
+                                  std::vector<int> &gtype) {
+    if (n_gates && (!gates || !param_index)) return fail(KBWG_EINVAL, "null gate list");
+    const uint64_t all = (s->n >= 64) ? ~0ull : ((1ull << s->n) - 1);
+    fwd.resize(n_gates);
+    angles.resize(n_gates);
+    gtype.assign(n_gates, GT_NONE);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ || g.target >= s->n || (g.control_mask & ~all) || (g.control_mask & (1ull << g.target)))
+            return fail(KBWG_EINVAL, "bad gate");
+        fwd[i] = make_gate_desc(s->prec, g.kind, g.target, g.control_mask, g.angle);
+        angles[i] = g.angle;
+        const int32_t pi = param_index[i];
+        if (pi >= 0) {
+            if ((uintptr_t)pi >= n_params) return fail(KBWG_EINVAL, "param_index out of range");
+            switch (g.kind) {
+            case KBWG_RX: gtype[i] = GT_X; break;
+            case KBWG_RY: gtype[i] = GT_Y; break;
+            case KBWG_RZ: gtype[i] = GT_Z; break;
+            case KBWG_P: gtype[i] = GT_P1; break;
+            default: return fail(KBWG_EINVAL, "only P, RX, RY, RZ gates take a parameter");
+            }
+        } else if (pi != -1) {
+            return fail(KBWG_EINVAL, "param_index must be -1 or a parameter index");
+        }
+    }
+    return KBWG_OK;
+}
+
+extern "C" {
+
+int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubits, const uintptr_t *offsets,
+                       const double *coefficients, uintptr_t n_strings, double *out) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!out) return fail(KBWG_EINVAL, "null output");
+    std::vector<PauliString> strs;
+    int32_t r = parse_hamiltonian(s->n, paulis, qubits, offsets, coefficients, n_strings, strs);
+    if (r) return r;
+    CUDA_TRY(flush_queue(*s));
+    return exp_value_core(s, strs, out);
+    GUARD_END
+}
+
+int32_t kbwg_adjoint_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates, const int32_t *param_index,
+                              uintptr_t n_params, const uint8_t *paulis, const uintptr_t *qubits,
+                              const uintptr_t *offsets, const double *coefficients, uintptr_t n_strings,
+                              uint32_t max_checkpoints, double *energy, double *gradient) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!energy || (n_params && !gradient)) return fail(KBWG_EINVAL, "null output");
+    std::vector<PauliString> strs;
+    int32_t r = parse_hamiltonian(s->n, paulis, qubits, offsets, coefficients, n_strings, strs);
+    if (r) return r;
+    std::vector<GateDesc> fwd;
+    std::vector<double> angles;
+    std::vector<int> gtype;
+    r = parse_grad_circuit(s, gates, n_gates, param_index, n_params, fwd, angles, gtype);
+    if (r) return r;
+    CUDA_TRY(flush_queue(*s));
+    std::vector<double> per_gate;
+    r = adjoint_gradient(*s, fwd, angles, gtype, strs, energy, per_gate, max_checkpoints);
+    if (r) return r;
+    for (uintptr_t p = 0; p < n_params; p++) gradient[p] = 0.0;
+    for (uintptr_t i = 0; i < n_gates; i++)
+        if (param_index[i] >= 0) gradient[param_index[i]] += per_gate[i];
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_param_shift_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates,
+                                  const int32_t *param_index, uintptr_t n_params, const uint8_t *paulis,
+                                  const uintptr_t *qubits, const uintptr_t *offsets, const double *coefficients,
+                                  uintptr_t n_strings, double *energy, double *gradient) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (!energy || (n_params && !gradient)) return fail(KBWG_EINVAL, "null output");
+    std::vector<PauliString> strs;
+    int32_t r = parse_hamiltonian(s->n, paulis, qubits, offsets, coefficients, n_strings, strs);
+    if (r) return r;
+    std::vector<GateDesc> fwd;
+    std::vector<double> angles;
+    std::vector<int> gtype;
+    r = parse_grad_circuit(s, gates, n_gates, param_index, n_params, fwd, angles, gtype);
+    if (r) return r;
+    for (uintptr_t i = 0; i < n_gates; i++)
+        if (gtype[i] != GT_NONE && gates[i].control_mask)
+            return fail(KBWG_EINVAL, "the +-pi/2 shift rule needs uncontrolled parameterised gates");
+    // one fresh evaluation per circuit, as BatchExecution::exp_value does
+    // (src/quantum_execution.rs:392-405)
+    auto evaluate = [&](const std::vector<GateDesc> &circ, double *e) -> int32_t {
+        s->queue.clear();
+        CUDA_TRY(dispatch(s, [&](auto *tp) {
+            using T = std::remove_pointer_t<decltype(tp)>;
+            return launch_init<T>(s->state, s->n, s->stream);
+        }));
+        s->queue = circ;
+        CUDA_TRY(flush_queue(*s));
+        return exp_value_core(s, strs, e);
+    };
+    r = evaluate(fwd, energy);
+    if (r) return r;
+    for (uintptr_t p = 0; p < n_params; p++) gradient[p] = 0.0;
+    const double shift = 1.57079632679489661923;  // pi/2
+    std::vector<GateDesc> circ = fwd;
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        if (gtype[i] == GT_NONE) continue;
+        double ep = 0.0, em = 0.0;
+        circ[i] = make_gate_desc(s->prec, gates[i].kind, gates[i].target, gates[i].control_mask, angles[i] + shift);
+        r = evaluate(circ, &ep);
+        if (r) return r;
+        circ[i] = make_gate_desc(s->prec, gates[i].kind, gates[i].target, gates[i].control_mask, angles[i] - shift);
+        r = evaluate(circ, &em);
+        if (r) return r;
+        circ[i] = fwd[i];
+        gradient[param_index[i]] += 0.5 * (ep - em);
+    }
     return KBWG_OK;
     GUARD_END
 }

@@ -129,17 +129,17 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                 TileGate t;
                 memset(&t, 0, sizeof t);
                 switch (x.kind) {
-                case G_X: t.cls = TG_PERM; t.sub = 0; break;
-                case G_Y: t.cls = TG_PERM; t.sub = 1; break;
+                case G_X: t.cls = TG_X; break;
+                case G_Y: t.cls = TG_Y; break;
                 case G_H: t.cls = TG_H; break;
-                case G_RY: t.cls = TG_ROT; t.sub = 0; break;
-                case G_RX: t.cls = TG_ROT; t.sub = 1; break;
-                case G_Z: t.cls = TG_DIAG; t.sub = 0; break;
-                case G_P: t.cls = TG_DIAG; t.sub = 1; break;
-                case G_RZ: t.cls = TG_DIAG; t.sub = 2; break;
                 case G_HN: t.cls = TG_H; t.sub = 1; break;
-                case G_PI: t.cls = TG_DIAG; t.sub = 3; break;
-                default: t.cls = TG_DIAG; t.sub = 5; break;  // G_SCALE
+                case G_RX: t.cls = TG_RX; break;
+                case G_RY: t.cls = TG_RY; break;
+                case G_Z: t.cls = TG_Z; break;
+                case G_P: t.cls = TG_P; break;
+                case G_RZ: t.cls = TG_RZ; break;
+                case G_PI: t.cls = TG_PI; break;
+                default: t.cls = TG_SCALE; break;
                 }
                 memcpy(t.c, x.c, sizeof t.c);
                 const int lb = local_bit(sw, x.target);

@@ -82,6 +82,23 @@ cudaError_t flush_queue(Sim &s);
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
 
 double next_draw(Sim &s);
+
+// A parsed Pauli string: P = i^{ny} X^x Z^z (per qubit), with its coefficient.
+struct PauliString {
+    uint64_t x = 0, z = 0;
+    int ny = 0;
+    double coef = 0.0;
+};
+
+// Gradient types of the adjoint sweep.
+enum { GT_NONE = 0, GT_X = 1, GT_Y = 2, GT_Z = 3, GT_P1 = 4 };
+
+// Adjoint gradient (adjoint.cu).  fwd: the circuit; angles: each gate's
+// angle; gtype: GT_* per gate (GT_NONE if not differentiated).  Writes E and
+// dE/dtheta per gate; the handle ends in |0...0>.  Returns 0 or a KBWG_* code.
+int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
+                         const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
+                         std::vector<double> &grad_per_gate, uint32_t max_ckpt);
 double host_uniform_scale(double total);
 
 }  // namespace kbwg

@@ -17,19 +17,26 @@ constexpr int kMaxSweepGates = 256; // gates per sweep (the program is staged in
 // thread, 32 * 2^(K-5-R) threads per CTA.
 template <class T> struct TileCfg;
 template <> struct TileCfg<float> {
-    static constexpr int K = 13, R = 5;
+    static constexpr int K = 13, R = 4;
 };
 template <> struct TileCfg<double> {
     static constexpr int K = 12, R = 4;
 };
 
-// Arithmetic classes of the trait gates.
+// Arithmetic classes of the gates, one per code path of the tile kernels.
 enum {
-    TG_PERM = 0,  // X (sub 0), Y (sub 1): permutation with sign/i factors
-    TG_H = 1,     // Hadamard: (a0 +- a1) * c0
-    TG_ROT = 2,   // RY (sub 0), RX (sub 1): c*a + s*T(partner)
-    TG_DIAG = 3   // Z (sub 0), P (sub 1: a1 * (c0,c1)), RZ (sub 2: a0 * (c0,c1), a1 * (c2,c3))
+    TG_X = 0,      // swap
+    TG_Y = 1,      // a0' = -i a1, a1' = i a0
+    TG_H = 2,      // (a0 +- a1) * c0 (sub 0); sub 1: without the factor (float-float path)
+    TG_RX = 3,     // c a - i s partner
+    TG_RY = 4,     // c a -+ s partner
+    TG_Z = 5,      // |1> negated (first diagonal class)
+    TG_P = 6,      // |1> * (c0 + i c1)
+    TG_RZ = 7,     // |0> * (c0 + i c1), |1> * (c2 + i c3)
+    TG_PI = 8,     // |1> * i^q, q = c0 (float-float path)
+    TG_SCALE = 9   // every amplitude * (c0 + i c1) (float-float path)
 };
+__host__ __device__ inline bool tg_diagonal(uint32_t cls) { return cls >= TG_Z; }
 constexpr uint8_t TG_OUTER = 0xFF;  // tb value: diagonal gate whose target lies outside the tile
 
 // One gate as a tile sees it (48 bytes; staged in shared memory).

@@ -48,16 +48,24 @@ __device__ __forceinline__ uint64_t insert_zero_at(uint64_t i, uint32_t m) {
     return ((i & ~low) << 1) | (i & low);
 }
 
-// ---- exact arithmetic policy (reference operation order) ----------------------
+// ---- arithmetic policies ----------------------------------------------------------
+// A policy supplies the amplitude type in registers (Amp) and in HBM (Mem),
+// the per-gate constants (K4), and one function per gate class.  *_pair
+// updates both amplitudes of a pair held by one thread; *_half returns the new
+// value of one side (`self`) given the other side (`o`) from another lane.
+
+// Exact: the reference's per-amplitude operations, each product and sum
+// rounded separately (no FMA contraction): bit-identical to Dense<F>.
 template <class T>
 struct Exact {
     using Amp = cx<T>;
-    using Mem = cx<T>;  // amplitude format in HBM
+    using Mem = cx<T>;
+    using Scalar = T;
     static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
     // Constants are stored in T on the host (exact: they are T values widened
-    // to double), so no thread converts precision at run time (a float<->double
-    // conversion issues at the FP64 rate on this chip).
+    // to double), so no thread converts precision at run time (a
+    // float<->double conversion issues at the FP64 rate on this chip).
     static void pack_host(TileGate &g) {
         T v[4];
         for (int i = 0; i < 4; i++) v[i] = (T)g.c[i];
@@ -72,76 +80,70 @@ struct Exact {
         return K4{v[0], v[1], v[2], v[3]};
     }
     static __device__ __forceinline__ Amp shfl(Amp v, int m) {
-        Amp r;
-        r.re = __shfl_xor_sync(0xffffffffu, v.re, m);
-        r.im = __shfl_xor_sync(0xffffffffu, v.im, m);
-        return r;
+        return Amp{__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m)};
     }
-    // X: swap.  Y: a0' = a1*(-i) = (a1.im, -a1.re), a1' = a0*i = (-a0.im, a0.re).
-    static __device__ __forceinline__ void perm_pair(int sub, Amp &a0, Amp &a1) {
-        if (sub == 0) {
-            const Amp t = a0;
-            a0 = a1;
-            a1 = t;
-        } else {
-            const Amp n0{a1.im, xneg(a1.re)}, n1{xneg(a0.im), a0.re};
-            a0 = n0;
-            a1 = n1;
-        }
+    static __device__ __forceinline__ Amp neg(Amp a) { return Amp{-a.re, -a.im}; }
+    // Y: a0' = a1*(-i) = (a1.im, -a1.re), a1' = a0*i = (-a0.im, a0.re)
+    static __device__ __forceinline__ void y_pair(Amp &a0, Amp &a1) {
+        const Amp n0{a1.im, -a1.re}, n1{-a0.im, a0.re};
+        a0 = n0;
+        a1 = n1;
     }
-    static __device__ __forceinline__ Amp perm_half(int sub, Amp o, bool one) {
-        if (sub == 0) return o;
-        return one ? Amp{xneg(o.im), o.re} : Amp{o.im, xneg(o.re)};
+    static __device__ __forceinline__ Amp y_half(Amp o, bool one) {
+        return one ? Amp{-o.im, o.re} : Amp{o.im, -o.re};
     }
-    // H: a0' = (a0 + a1) * h, a1' = (a0 - a1) * h
+    // H: a0' = (a0 + a1) h, a1' = (a0 - a1) h
     static __device__ __forceinline__ void h_pair(int, const K4 &k, Amp &a0, Amp &a1) {
         const Amp n0{xmul(xadd(a0.re, a1.re), k.c0), xmul(xadd(a0.im, a1.im), k.c0)};
         const Amp n1{xmul(xsub(a0.re, a1.re), k.c0), xmul(xsub(a0.im, a1.im), k.c0)};
         a0 = n0;
         a1 = n1;
     }
-    static __device__ __forceinline__ Amp h_half(int, const K4 &k, Amp self, Amp o, bool one) {
-        return one ? Amp{xmul(xsub(o.re, self.re), k.c0), xmul(xsub(o.im, self.im), k.c0)}
-                   : Amp{xmul(xadd(self.re, o.re), k.c0), xmul(xadd(self.im, o.im), k.c0)};
+    // sgn = +1 on the |0> side, -1 on the |1> side: (o + sgn*self) rounds
+    // exactly like self + o resp. o - self, and sgn*self is exact, so one FMA
+    // gives the reference's sum.
+    static __device__ __forceinline__ Amp h_half(int, const K4 &k, Amp self, Amp o, T sgn) {
+        return Amp{xmul(fma(sgn, self.re, o.re), k.c0), xmul(fma(sgn, self.im, o.im), k.c0)};
     }
-    // RY/RX: x' = c*x + s*t, t = -partner (RY, |0> side), +partner (RY, |1>
-    // side), or (partner.im, -partner.re) (RX, either side); the same roundings
-    // as the reference's c*x -/+ s*y forms.
-    static __device__ __forceinline__ Amp rot_t(int sub, Amp o, bool one) {
-        if (sub == 1) return Amp{o.im, xneg(o.re)};
-        return one ? o : Amp{xneg(o.re), xneg(o.im)};
-    }
-    static __device__ __forceinline__ Amp rot_mix(const K4 &k, Amp x, Amp t) {
-        return Amp{xadd(xmul(k.c0, x.re), xmul(k.c1, t.re)), xadd(xmul(k.c0, x.im), xmul(k.c1, t.im))};
-    }
-    static __device__ __forceinline__ void rot_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
-        const Amp n0 = rot_mix(k, a0, rot_t(sub, a1, false));
-        const Amp n1 = rot_mix(k, a1, rot_t(sub, a0, true));
+    // RX: a0' = (c a0.re + s a1.im, c a0.im - s a1.re), a1' symmetric
+    static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const Amp n0{xadd(xmul(k.c0, a0.re), xmul(k.c1, a1.im)), xsub(xmul(k.c0, a0.im), xmul(k.c1, a1.re))};
+        const Amp n1{xadd(xmul(k.c0, a1.re), xmul(k.c1, a0.im)), xsub(xmul(k.c0, a1.im), xmul(k.c1, a0.re))};
         a0 = n0;
         a1 = n1;
     }
-    static __device__ __forceinline__ Amp rot_half(int sub, const K4 &k, Amp self, Amp o, bool one) {
-        return rot_mix(k, self, rot_t(sub, o, one));
+    static __device__ __forceinline__ Amp rx_half(const K4 &k, Amp self, Amp o) {
+        return Amp{xadd(xmul(k.c0, self.re), xmul(k.c1, o.im)), xsub(xmul(k.c0, self.im), xmul(k.c1, o.re))};
     }
-    // Z: negate the |1> amplitude; P: |1> * (c0 + i c1); RZ: |0> * (c0 + i c1), |1> * (c2 + i c3).
-    static __device__ __forceinline__ Amp diag(int sub, const K4 &k, Amp a, bool one) {
-        if (sub == 0) return one ? Amp{xneg(a.re), xneg(a.im)} : a;
-        if (sub == 1) return one ? cmul_exact(a, k.c0, k.c1) : a;
-        return one ? cmul_exact(a, k.c2, k.c3) : cmul_exact(a, k.c0, k.c1);
+    // RY: a0' = c a0 - s a1, a1' = c a1 + s a0
+    static __device__ __forceinline__ void ry_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const Amp n0{xsub(xmul(k.c0, a0.re), xmul(k.c1, a1.re)), xsub(xmul(k.c0, a0.im), xmul(k.c1, a1.im))};
+        const Amp n1{xadd(xmul(k.c0, a1.re), xmul(k.c1, a0.re)), xadd(xmul(k.c0, a1.im), xmul(k.c1, a0.im))};
+        a0 = n0;
+        a1 = n1;
     }
+    // ss = +s on the |1> side, -s on the |0> side: c x + (-s) o == c x - s o
+    static __device__ __forceinline__ T signed_s(const K4 &k, bool one) { return one ? k.c1 : -k.c1; }
+    static __device__ __forceinline__ T sign(bool one) { return one ? (T)-1 : (T)1; }
+    static __device__ __forceinline__ Amp ry_half(const K4 &k, Amp self, Amp o, T ss) {
+        return Amp{xadd(xmul(k.c0, self.re), xmul(ss, o.re)), xadd(xmul(k.c0, self.im), xmul(ss, o.im))};
+    }
+    static __device__ __forceinline__ Amp cmul(Amp a, T c, T s) { return cmul_exact(a, c, s); }
+    static __device__ __forceinline__ Amp pi_mul(Amp a, int) { return a; }  // float-float path only
 };
 
 // ---- float-float policy (complex128 fast path) ---------------------------------
 // HBM keeps IEEE binary64; amplitudes become hi+lo float pairs on the way in
 // and are rounded back on the way out.  Constants arrive pre-split by
-// pack_host.  Extra classes used only here: H sub 1 (no 1/sqrt(2): the host
-// folds it into a final scale gate), DIAG sub 3 (|1> times i^q, free) and
-// DIAG sub 5 (every amplitude times c0 + i c1, the folded global factor).
+// pack_host.  Classes used only here: H sub 1 (no 1/sqrt(2): the host folds
+// it into a final scale gate), PI (|1> times i^q, free) and SCALE (every
+// amplitude times c0 + i c1, the folded global factor).
 struct FFPol {
     struct Amp {
         ff::f2 re, im;
     };
     using Mem = cx<double>;
+    using Scalar = ff::f2;
     struct K4 {
         ff::f2 c0, c1, c2, c3;
     };
@@ -170,19 +172,13 @@ struct FFPol {
         r.im.l = __shfl_xor_sync(0xffffffffu, v.im.l, m);
         return r;
     }
-    static __device__ __forceinline__ void perm_pair(int sub, Amp &a0, Amp &a1) {
-        if (sub == 0) {
-            const Amp t = a0;
-            a0 = a1;
-            a1 = t;
-        } else {
-            const Amp n0{a1.im, ff::neg(a1.re)}, n1{ff::neg(a0.im), a0.re};
-            a0 = n0;
-            a1 = n1;
-        }
+    static __device__ __forceinline__ Amp neg(Amp a) { return Amp{ff::neg(a.re), ff::neg(a.im)}; }
+    static __device__ __forceinline__ void y_pair(Amp &a0, Amp &a1) {
+        const Amp n0{a1.im, ff::neg(a1.re)}, n1{ff::neg(a0.im), a0.re};
+        a0 = n0;
+        a1 = n1;
     }
-    static __device__ __forceinline__ Amp perm_half(int sub, Amp o, bool one) {
-        if (sub == 0) return o;
+    static __device__ __forceinline__ Amp y_half(Amp o, bool one) {
         return one ? Amp{ff::neg(o.im), o.re} : Amp{o.im, ff::neg(o.re)};
     }
     static __device__ __forceinline__ void h_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
@@ -195,74 +191,156 @@ struct FFPol {
         a0 = n0;
         a1 = n1;
     }
-    static __device__ __forceinline__ Amp h_half(int sub, const K4 &k, Amp self, Amp o, bool one) {
+    // sgn = (+1, 0) or (-1, 0): o + sgn*self
+    static __device__ __forceinline__ Amp h_half(int sub, const K4 &k, Amp self, Amp o, ff::f2 sgn) {
+        const bool one = sgn.h < 0.f;
         Amp r = one ? Amp{ff::sub(o.re, self.re), ff::sub(o.im, self.im)}
                     : Amp{ff::add(self.re, o.re), ff::add(self.im, o.im)};
         if (sub == 0) r = Amp{ff::mul(r.re, k.c0), ff::mul(r.im, k.c0)};
         return r;
     }
-    static __device__ __forceinline__ Amp rot_t(int sub, Amp o, bool one) {
-        if (sub == 1) return Amp{o.im, ff::neg(o.re)};
-        return one ? o : Amp{ff::neg(o.re), ff::neg(o.im)};
-    }
-    static __device__ __forceinline__ Amp rot_mix(const K4 &k, Amp x, Amp t) {
-        return Amp{ff::dot2(k.c0, x.re, k.c1, t.re), ff::dot2(k.c0, x.im, k.c1, t.im)};
-    }
-    static __device__ __forceinline__ void rot_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
-        const Amp n0 = rot_mix(k, a0, rot_t(sub, a1, false));
-        const Amp n1 = rot_mix(k, a1, rot_t(sub, a0, true));
+    static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const ff::f2 ns = ff::neg(k.c1);
+        const Amp n0{ff::dot2(k.c0, a0.re, k.c1, a1.im), ff::dot2(k.c0, a0.im, ns, a1.re)};
+        const Amp n1{ff::dot2(k.c0, a1.re, k.c1, a0.im), ff::dot2(k.c0, a1.im, ns, a0.re)};
         a0 = n0;
         a1 = n1;
     }
-    static __device__ __forceinline__ Amp rot_half(int sub, const K4 &k, Amp self, Amp o, bool one) {
-        return rot_mix(k, self, rot_t(sub, o, one));
+    static __device__ __forceinline__ Amp rx_half(const K4 &k, Amp self, Amp o) {
+        return Amp{ff::dot2(k.c0, self.re, k.c1, o.im), ff::dot2(k.c0, self.im, ff::neg(k.c1), o.re)};
+    }
+    static __device__ __forceinline__ void ry_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const ff::f2 ns = ff::neg(k.c1);
+        const Amp n0{ff::dot2(k.c0, a0.re, ns, a1.re), ff::dot2(k.c0, a0.im, ns, a1.im)};
+        const Amp n1{ff::dot2(k.c0, a1.re, k.c1, a0.re), ff::dot2(k.c0, a1.im, k.c1, a0.im)};
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ ff::f2 signed_s(const K4 &k, bool one) { return one ? k.c1 : ff::neg(k.c1); }
+    static __device__ __forceinline__ ff::f2 sign(bool one) { return one ? ff::f2{-1.f, 0.f} : ff::f2{1.f, 0.f}; }
+    static __device__ __forceinline__ Amp ry_half(const K4 &k, Amp self, Amp o, ff::f2 ss) {
+        return Amp{ff::dot2(k.c0, self.re, ss, o.re), ff::dot2(k.c0, self.im, ss, o.im)};
     }
     static __device__ __forceinline__ Amp cmul(Amp a, ff::f2 c, ff::f2 s) {
         return Amp{ff::dot2(c, a.re, ff::neg(s), a.im), ff::dot2(c, a.im, s, a.re)};
     }
-    static __device__ __forceinline__ Amp diag(int sub, const K4 &k, Amp a, bool one) {
-        switch (sub) {
-        case 0: return one ? Amp{ff::neg(a.re), ff::neg(a.im)} : a;
-        case 1: return one ? cmul(a, k.c0, k.c1) : a;
-        case 2: return one ? cmul(a, k.c2, k.c3) : cmul(a, k.c0, k.c1);
-        case 3: {
-            if (!one) return a;
-            const int q = (int)k.c0.h;
-            if (q == 1) return Amp{ff::neg(a.im), a.re};
-            if (q == 2) return Amp{ff::neg(a.re), ff::neg(a.im)};
-            return Amp{a.im, ff::neg(a.re)};
-        }
-        default: return cmul(a, k.c0, k.c1);
-        }
+    static __device__ __forceinline__ Amp pi_mul(Amp a, int q) {
+        if (q == 1) return Amp{ff::neg(a.im), a.re};
+        if (q == 2) return Amp{ff::neg(a.re), ff::neg(a.im)};
+        return Amp{a.im, ff::neg(a.re)};
     }
 };
 
+// ---- per-gate register code -------------------------------------------------------
+#define KBWG_CTRL_OK(j) (creg == 0u || ((uint32_t)(j) & creg) == creg)
+
+// Gate on register bit B: 2^(R-1) in-thread pairs.
 template <class P, int R, int B, int CLS>
-__device__ __forceinline__ void reg_pairs(typename P::Amp (&v)[1 << R], const TileGate &g,
-                                          const typename P::K4 &k, uint32_t creg) {
-    // creg == 0 (no control on a register bit) is the common case: no
-    // per-pair test at all
+__device__ __forceinline__ void reg_pairs(typename P::Amp (&v)[1 << R], int sub, const typename P::K4 &k,
+                                          uint32_t creg) {
 #pragma unroll
     for (int jj = 0; jj < (1 << (R - 1)); jj++) {
         const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
         const int j1 = j0 | (1 << B);
-        if (creg == 0u || ((uint32_t)j0 & creg) == creg) {
-            if (CLS == TG_PERM) P::perm_pair(g.sub, v[j0], v[j1]);
-            if (CLS == TG_H) P::h_pair(g.sub, k, v[j0], v[j1]);
-            if (CLS == TG_ROT) P::rot_pair(g.sub, k, v[j0], v[j1]);
+        if (KBWG_CTRL_OK(j0)) {
+            if (CLS == TG_X) {
+                const typename P::Amp t = v[j0];
+                v[j0] = v[j1];
+                v[j1] = t;
+            }
+            if (CLS == TG_Y) P::y_pair(v[j0], v[j1]);
+            if (CLS == TG_H) P::h_pair(sub, k, v[j0], v[j1]);
+            if (CLS == TG_RX) P::rx_pair(k, v[j0], v[j1]);
+            if (CLS == TG_RY) P::ry_pair(k, v[j0], v[j1]);
         }
     }
 }
 
 template <class P, int R, int CLS>
-__device__ __forceinline__ void reg_gate(typename P::Amp (&v)[1 << R], const TileGate &g, const typename P::K4 &k,
-                                         int b, uint32_t creg) {
+__device__ __forceinline__ void reg_gate(typename P::Amp (&v)[1 << R], int sub, const typename P::K4 &k, int b,
+                                         uint32_t creg) {
     switch (b) {
-    case 0: reg_pairs<P, R, 0, CLS>(v, g, k, creg); break;
-    case 1: reg_pairs<P, R, 1, CLS>(v, g, k, creg); break;
-    case 2: reg_pairs<P, R, 2, CLS>(v, g, k, creg); break;
-    case 3: reg_pairs<P, R, 3, CLS>(v, g, k, creg); break;
-    default: reg_pairs<P, R, R - 1, CLS>(v, g, k, creg); break;
+    case 0: reg_pairs<P, R, 0, CLS>(v, sub, k, creg); break;
+    case 1: reg_pairs<P, R, 1, CLS>(v, sub, k, creg); break;
+    case 2: reg_pairs<P, R, 2, CLS>(v, sub, k, creg); break;
+    case 3:
+        if constexpr (R > 3) reg_pairs<P, R, (R > 3 ? 3 : 0), CLS>(v, sub, k, creg);
+        break;
+    default:
+        if constexpr (R > 4) reg_pairs<P, R, (R > 4 ? 4 : 0), CLS>(v, sub, k, creg);
+        break;
+    }
+}
+
+// Diagonal gate on register bit B: the side of every register is known at
+// compile time.
+template <class P, int R, int B>
+__device__ __forceinline__ void diag_reg(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
+                                         uint32_t creg) {
+    constexpr int NR = 1 << R;
+    switch (cls) {
+    case TG_Z:
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if ((j >> B) & 1)
+                if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
+        break;
+    case TG_P:
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if ((j >> B) & 1)
+                if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
+        break;
+    case TG_RZ:
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = ((j >> B) & 1) ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1);
+        break;
+    default: {  // TG_PI
+        const int q = (int)reinterpret_cast<const float &>(k.c0);
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if ((j >> B) & 1)
+                if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
+        break;
+    }
+    }
+}
+
+// Diagonal gate whose target bit is the same for all of this thread's
+// registers (a lane/warp bit, or a qubit outside the tile): `one` is uniform.
+template <class P, int R>
+__device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
+                                           uint32_t creg, bool one) {
+    constexpr int NR = 1 << R;
+    if (cls == TG_SCALE) {
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
+        return;
+    }
+    if (cls == TG_RZ) {
+        const auto c = one ? k.c2 : k.c0;
+        const auto s = one ? k.c3 : k.c1;
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], c, s);
+        return;
+    }
+    if (!one) return;
+    if (cls == TG_Z) {
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
+    } else if (cls == TG_P) {
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
+    } else {  // TG_PI
+        const int q = (int)reinterpret_cast<const float &>(k.c0);
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
     }
 }
 
@@ -271,67 +349,100 @@ __device__ __forceinline__ void reg_gate(typename P::Amp (&v)[1 << R], const Til
 template <class P, int K, int R>
 __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int R0, uint32_t F,
                                           uint64_t base) {
-    static_assert(R == 4 || R == 5, "reg_gate covers register bits 0..4");
+    static_assert(R >= 3 && R <= 5, "register bits 0..4");
     constexpr int NR = 1 << R;
     if ((base & g.co) != g.co) return;  // a control outside the tile is 0 for the whole tile
     const uint32_t regmask = (uint32_t)(NR - 1) << R0;
     const uint32_t fixed_need = g.cl & ~regmask;
     const bool fok = (F & fixed_need) == fixed_need;  // controls on this thread's lane/warp bits
     const uint32_t tb = g.tb;
-    const bool lane_target = g.cls != TG_DIAG && tb < (uint32_t)kLaneBits;
+    const uint32_t cls = g.cls;
+    const bool lane_target = !tg_diagonal(cls) && tb < (uint32_t)kLaneBits;
     // Threads whose lane/warp controls are 0 leave, except for lane-bit
     // targets: there every lane must take part in the warp shuffle.
     if (!fok && !lane_target) return;
     const typename P::K4 k = P::load(g);
     const uint32_t creg = (g.cl & regmask) >> R0;
-    if (g.cls == TG_DIAG) {
-        const int rb = (int)tb - R0;
-        if (tb != TG_OUTER && rb >= 0 && rb < R) {  // target bit is a register bit
+    if (lane_target) {
+        // partner in lane F ^ (1 << tb); a control never sits on the target
+        // bit, so both halves of a pair see the same control values
+        const bool one = ((F >> tb) & 1u) != 0;
+        const int m = 1 << tb;
+        switch (cls) {
+        case TG_X:
 #pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (creg == 0u || ((uint32_t)j & creg) == creg) v[j] = P::diag(g.sub, k, v[j], ((j >> rb) & 1) != 0);
-        } else {  // target fixed for this thread (lane/warp bit) or for the whole tile
-            const bool one = (tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0) : (((F >> tb) & 1u) != 0);
+            for (int j = 0; j < NR; j++) {
+                const typename P::Amp o = P::shfl(v[j], m);
+                if (fok && KBWG_CTRL_OK(j)) v[j] = o;
+            }
+            break;
+        case TG_Y:
 #pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (creg == 0u || ((uint32_t)j & creg) == creg) v[j] = P::diag(g.sub, k, v[j], one);
+            for (int j = 0; j < NR; j++) {
+                const typename P::Amp o = P::shfl(v[j], m);
+                if (fok && KBWG_CTRL_OK(j)) v[j] = P::y_half(o, one);
+            }
+            break;
+        case TG_H: {
+            const auto sg = P::sign(one);
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const typename P::Amp o = P::shfl(v[j], m);
+                if (fok && KBWG_CTRL_OK(j)) v[j] = P::h_half(g.sub, k, v[j], o, sg);
+            }
+            break;
+        }
+        case TG_RX:
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const typename P::Amp o = P::shfl(v[j], m);
+                if (fok && KBWG_CTRL_OK(j)) v[j] = P::rx_half(k, v[j], o);
+            }
+            break;
+        default: {  // TG_RY
+            const auto ss = P::signed_s(k, one);
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const typename P::Amp o = P::shfl(v[j], m);
+                if (fok && KBWG_CTRL_OK(j)) v[j] = P::ry_half(k, v[j], o, ss);
+            }
+            break;
+        }
         }
         return;
     }
-    if (lane_target) {
-        // partner lives in lane F ^ (1 << tb); a control on a lane bit has the
-        // same value on both halves of a pair (it is never the target bit)
-        const bool one = ((F >> tb) & 1u) != 0;
-        const int m = 1 << tb;
-        if (g.cls == TG_PERM) {
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && (creg == 0u || ((uint32_t)j & creg) == creg)) v[j] = P::perm_half(g.sub, o, one);
-            }
-        } else if (g.cls == TG_H) {
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && (creg == 0u || ((uint32_t)j & creg) == creg)) v[j] = P::h_half(g.sub, k, v[j], o, one);
+    if (tg_diagonal(cls)) {
+        const int rb = (int)tb - R0;
+        if (cls != TG_SCALE && tb != TG_OUTER && rb >= 0 && rb < R) {
+            switch (rb) {
+            case 0: diag_reg<P, R, 0>(v, cls, k, creg); break;
+            case 1: diag_reg<P, R, 1>(v, cls, k, creg); break;
+            case 2: diag_reg<P, R, 2>(v, cls, k, creg); break;
+            case 3:
+                if constexpr (R > 3) diag_reg<P, R, (R > 3 ? 3 : 0)>(v, cls, k, creg);
+                break;
+            default:
+                if constexpr (R > 4) diag_reg<P, R, (R > 4 ? 4 : 0)>(v, cls, k, creg);
+                break;
             }
         } else {
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && (creg == 0u || ((uint32_t)j & creg) == creg)) v[j] = P::rot_half(g.sub, k, v[j], o, one);
-            }
+            const bool one = (cls == TG_SCALE) ? true
+                             : (tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0)
+                                                : (((F >> tb) & 1u) != 0);
+            diag_fixed<P, R>(v, cls, k, creg, one);
         }
         return;
     }
     const int b = (int)tb - R0;
-    if (g.cls == TG_PERM)
-        reg_gate<P, R, TG_PERM>(v, g, k, b, creg);
-    else if (g.cls == TG_H)
-        reg_gate<P, R, TG_H>(v, g, k, b, creg);
-    else
-        reg_gate<P, R, TG_ROT>(v, g, k, b, creg);
+    switch (cls) {
+    case TG_X: reg_gate<P, R, TG_X>(v, g.sub, k, b, creg); break;
+    case TG_Y: reg_gate<P, R, TG_Y>(v, g.sub, k, b, creg); break;
+    case TG_H: reg_gate<P, R, TG_H>(v, g.sub, k, b, creg); break;
+    case TG_RX: reg_gate<P, R, TG_RX>(v, g.sub, k, b, creg); break;
+    default: reg_gate<P, R, TG_RY>(v, g.sub, k, b, creg); break;
+    }
 }
 
+#undef KBWG_CTRL_OK
 
 }  // namespace kbwg

@@ -177,6 +177,34 @@ class DenseGB300:
     def clear(self):
         N.check(self._lib.kbwg_clear(self._h))
 
+    # -- gradients ------------------------------------------------------------------
+    def adjoint_gradient(self, circuit, param_index, n_params, hamiltonian, max_checkpoints=16):
+        """E = <psi|H|psi> and dE/dparams by the reverse-mode adjoint kernel.
+        param_index[i] is the parameter gate i's angle is (-1: constant)."""
+        ga = _gate_array(circuit)
+        pi = np.ascontiguousarray(param_index, dtype=np.int32)
+        pa, qa, oa, ca, ns = _ham_arrays(hamiltonian)
+        e = ctypes.c_double()
+        g = np.zeros(max(int(n_params), 1), np.float64)
+        N.check(self._lib.kbwg_adjoint_gradient(self._h, ga, len(circuit), _p(pi, ctypes.c_int32), int(n_params),
+                                                _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t),
+                                                _p(oa, ctypes.c_size_t), _p(ca, ctypes.c_double), ns,
+                                                int(max_checkpoints), ctypes.byref(e), _p(g, ctypes.c_double)))
+        return e.value, g[: int(n_params)]
+
+    def param_shift_gradient(self, circuit, param_index, n_params, hamiltonian):
+        """The same gradient by the parameter-shift rule on the GPU."""
+        ga = _gate_array(circuit)
+        pi = np.ascontiguousarray(param_index, dtype=np.int32)
+        pa, qa, oa, ca, ns = _ham_arrays(hamiltonian)
+        e = ctypes.c_double()
+        g = np.zeros(max(int(n_params), 1), np.float64)
+        N.check(self._lib.kbwg_param_shift_gradient(self._h, ga, len(circuit), _p(pi, ctypes.c_int32), int(n_params),
+                                                    _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t),
+                                                    _p(oa, ctypes.c_size_t), _p(ca, ctypes.c_double), ns,
+                                                    ctypes.byref(e), _p(g, ctypes.c_double)))
+        return e.value, g[: int(n_params)]
+
     # -- raw access -----------------------------------------------------------------
     def state(self):
         dt = _DT[self.prec][1]
@@ -228,6 +256,31 @@ class DenseGB300:
         p = ctypes.c_uint64()
         N.check(self._lib.kbwg_last_flush_stats(self._h, ctypes.byref(g), ctypes.byref(p)))
         return int(g.value), int(p.value)
+
+
+def _gate_array(circuit):
+    arr = (N.Gate * max(len(circuit), 1))()
+    for i, (kind, t, ctrl, ang) in enumerate(circuit):
+        m = 0
+        for c in ctrl:
+            m |= 1 << int(c)
+        arr[i] = N.Gate(int(kind), int(t), m, float(ang))
+    return arr
+
+
+def _ham_arrays(hamiltonian):
+    paulis, qubits, offsets, coefs = [], [], [0], []
+    for coef, terms in hamiltonian:
+        for p, q in terms:
+            paulis.append(int(p))
+            qubits.append(int(q))
+        offsets.append(len(paulis))
+        coefs.append(float(coef))
+    pa = np.ascontiguousarray(paulis if paulis else [0], dtype=np.uint8)
+    qa = np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp)
+    oa = np.ascontiguousarray(offsets, dtype=np.uintp)
+    ca = np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64)
+    return pa, qa, oa, ca, len(coefs)
 
 
 def plan(num_qubits, circuit, prec="c128", exact_order=False):

@@ -1,0 +1,125 @@
+"""Adjoint gradients (kbwg_adjoint_gradient) against the parameter-shift
+rule evaluated on the CPU oracle (restated Dense<f64>), against central
+finite differences, and against the GPU parameter-shift entry.  Tolerances
+follow the targets: <= 1e-10 (complex128), <= 1e-5 (complex64)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from kbw_gb300 import DenseGB300, KbwgError
+from kbw_gb300 import circuits as C
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_energy(n, circ, ham):
+    o = oracle.OracleDense(n, "c128")
+    o.apply(circ)
+    return o.exp_value(ham)
+
+
+def oracle_param_shift(n, circ, param_index, n_params, ham):
+    g = np.zeros(n_params)
+    for i, p in enumerate(param_index):
+        if p < 0:
+            continue
+        kind, t, c, a = circ[i]
+        plus = list(circ)
+        minus = list(circ)
+        plus[i] = (kind, t, c, a + math.pi / 2)
+        minus[i] = (kind, t, c, a - math.pi / 2)
+        g[p] += 0.5 * (oracle_energy(n, plus, ham) - oracle_energy(n, minus, ham))
+    return g
+
+
+@pytest.mark.parametrize("prec,fast,tol", [("c128", False, 1e-10), ("c128", True, 1e-10), ("c64", False, 1e-5)])
+def test_adjoint_hea_vs_oracle_param_shift(prec, fast, tol):
+    n, L = 12, 2
+    params = C.hea_params(n, L, 3)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    sim = DenseGB300(n, prec, fast_c128=fast)
+    e, g = sim.adjoint_gradient(circ, pidx, len(params), ham)
+    want = oracle_param_shift(n, circ, pidx, len(params), ham)
+    assert abs(e - oracle_energy(n, circ, ham)) < (1e-11 if prec == "c128" else 1e-5)
+    assert np.max(np.abs(g - want)) < tol, np.max(np.abs(g - want))
+
+
+def test_adjoint_checkpoints_do_not_change_result():
+    n, L = 13, 4
+    params = C.hea_params(n, L, 5)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    sim = DenseGB300(n, "c128")
+    e0, g0 = sim.adjoint_gradient(circ, pidx, len(params), ham, max_checkpoints=0)
+    e1, g1 = sim.adjoint_gradient(circ, pidx, len(params), ham, max_checkpoints=7)
+    assert abs(e0 - e1) < 1e-13 and np.max(np.abs(g0 - g1)) < 1e-12
+
+
+def test_adjoint_controlled_phase_shared_params_vs_finite_differences():
+    """Controlled rotations, phase gates and a parameter used by two gates:
+    compared with central differences (h = 1e-6) of the oracle energy."""
+    n = 12
+    rng = np.random.default_rng(9)
+    th = rng.uniform(-math.pi, math.pi, size=5)
+
+    def build(t):
+        c = [(C.H, q, (), 0.0) for q in range(n)]
+        c += [(C.RX, 3, (), t[0]), (C.RY, 7, (2,), t[1]), (C.P, 5, (), t[2]), (C.RZ, 11, (0, 4), t[3]),
+              (C.X, 6, (5,), 0.0), (C.RY, 1, (), t[4]), (C.P, 9, (8,), t[2]), (C.RX, 10, (), t[0])]
+        c += [(C.Z, (q + 1) % n, (q,), 0.0) for q in range(n)]
+        c += [(C.RY, q, (), 0.3 * q) for q in range(n)]
+        return c
+
+    pidx = [-1] * n + [0, 1, 2, 3, -1, 4, 2, 0] + [-1] * (2 * n)
+    ham = C.tfim_ring(n) + [(0.4, [(C.PAULI_Y, 2), (C.PAULI_X, 9)])]
+    sim = DenseGB300(n, "c128")
+    e, g = sim.adjoint_gradient(build(th), pidx, 5, ham)
+    h = 1e-6
+    fd = np.zeros(5)
+    for p in range(5):
+        tp, tm = th.copy(), th.copy()
+        tp[p] += h
+        tm[p] -= h
+        fd[p] = (oracle_energy(n, build(tp), ham) - oracle_energy(n, build(tm), ham)) / (2 * h)
+    assert abs(e - oracle_energy(n, build(th), ham)) < 1e-11
+    assert np.max(np.abs(g - fd)) < 1e-8, (g, fd)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_adjoint_vs_gpu_param_shift(prec):
+    n, L = 16, 3
+    params = C.hea_params(n, L, 7)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    sim = DenseGB300(n, prec)
+    e_a, g_a = sim.adjoint_gradient(circ, pidx, len(params), ham)
+    e_p, g_p = sim.param_shift_gradient(circ, pidx, len(params), ham)
+    tol = 1e-10 if prec == "c128" else 1e-5
+    assert abs(e_a - e_p) < tol and np.max(np.abs(g_a - g_p)) < tol
+
+
+def test_param_shift_rejects_controlled_rotations():
+    sim = DenseGB300(12, "c128")
+    circ = [(C.RY, 1, (0,), 0.3)]
+    with pytest.raises(KbwgError):
+        sim.param_shift_gradient(circ, [0], 1, C.tfim_ring(12))
+
+
+def test_torch_autograd_bridge():
+    torch = pytest.importorskip("torch")
+    from kbw_gb300.autograd import adjoint_energy
+    n, L = 12, 2
+    ham = C.tfim_ring(n)
+    sim = DenseGB300(n, "c128")
+    pidx = C.hea_param_index(n, L)
+    params = torch.tensor(C.hea_params(n, L, 11), dtype=torch.float64, requires_grad=True)
+    e = adjoint_energy(params, sim, lambda p: (C.hea(n, L, p), pidx), ham)
+    e.backward()
+    want = oracle_param_shift(n, C.hea(n, L, params.detach().numpy()), pidx, params.numel(), ham)
+    assert np.max(np.abs(params.grad.numpy() - want)) < 1e-10
