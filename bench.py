@@ -258,6 +258,37 @@ def run_adjoint_bench(args, torch, DenseGB300, C):
     return out
 
 
+def run_batch_bench(args, torch, C):
+    """Batched forward: 4096 hardware-efficient-ansatz circuits (n ~ U{8..20},
+    L ~ U{2..8}) in one persistent launch; circuits/s and the max |dE| of the
+    complex64 energies against the complex128 oracle on a sample."""
+    import oracle
+    from kbw_gb300 import batch_hea_tfim
+    circs = C.hea_batch(args.batch_circuits, seed=0)
+    batch_hea_tfim(circs[:64], prec="c64")  # warm-up
+    times = []
+    for _ in range(args.batch_reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = batch_hea_tfim(circs, prec="c64")
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    rng = np.random.default_rng(1)
+    small = [i for i, c in enumerate(circs) if c[0] <= 14]
+    sample = list(rng.choice(small, size=min(24, len(small)), replace=False))
+    sample += [i for i, c in enumerate(circs) if c[0] >= 19][:2]
+    err = 0.0
+    for i in sample:
+        n, L, p = circs[i]
+        o = oracle.OracleDense(n, "c128")
+        o.apply(C.hea(n, L, p))
+        err = max(err, abs(e[i] - o.exp_value(C.tfim_ring(n))))
+    return {"circuits": len(circs), "seconds": round(t, 5), "circuits_per_s": round(len(circs) / t, 1),
+            "max_abs_dE_vs_c128_oracle": err, "checked": len(sample), "precision": "c64",
+            "config": "hea-batch n~U{8..20} L~U{2..8} ring-TFIM, one persistent launch (incl. host<->device copies)"}
+
+
 def run_ours(args, world, rank, local):
     import torch
     import kbw_gb300
@@ -383,6 +414,8 @@ def run_ours(args, world, rank, local):
 
     if args.adjoint:
         secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C)
+    if args.batch:
+        secondary["batch"] = run_batch_bench(args, torch, C)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -429,6 +462,9 @@ def main():
     ap.add_argument("--ref-gates", type=int, default=4)
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
+    ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--batch-circuits", type=int, default=4096)
+    ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--adj-qubits", type=int, default=24)
     ap.add_argument("--adj-layers", type=int, default=10)
     ap.add_argument("--adj-reps", type=int, default=3)

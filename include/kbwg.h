@@ -180,6 +180,20 @@ int32_t kbwg_param_shift_gradient(kbwg_sim *sim, const kbwg_gate *gates, uintptr
                                   const uintptr_t *qubits, const uintptr_t *offsets, const double *coefficients,
                                   uintptr_t n_strings, double *energy, double *gradient);
 
+/* Many small variational circuits in one persistent launch.  Replaces the
+ * reference's one-fresh-simulator-per-request batch path
+ * (BatchExecution::exp_value, src/quantum_execution.rs:392-418) for the
+ * hardware-efficient ansatz: circuit c has num_qubits[c] (2..21) qubits and
+ * layers[c] layers of RY(theta) then RZ(phi) on every qubit followed by CZ on
+ * the ring (i, i+1 mod n); its 2 n L angles start at params[param_offset[c]]
+ * (per layer: the n RY angles, then the n RZ angles).  Writes
+ * <H> = zz sum <Z_i Z_i+1> + x sum <X_i> (ring) into energies[c].
+ * precision: KBWG_C64 or KBWG_C128 (flags: KBWG_FLAG_FAST_C128).  Runs on the
+ * current device, allocates its buffers per call. */
+int32_t kbwg_batch_hea_tfim(uintptr_t n_circuits, const uint32_t *num_qubits, const uint32_t *layers,
+                            const uint64_t *param_offset, const double *params, uintptr_t n_params, double zz,
+                            double x, int32_t precision, uint32_t flags, double *energies);
+
 /* QuantumExecution::clear (src/quantum_execution.rs:161; src/dense.rs:399-406). */
 int32_t kbwg_clear(kbwg_sim *sim);
 

@@ -5,5 +5,5 @@ sm_103a behind the C ABI of include/kbwg.h.
 ``DenseGB300`` mirrors the reference's ``QuantumExecution`` trait; the
 workload generators live in ``kbw_gb300.circuits``.
 """
-from .dense import DenseGB300, plan  # noqa: F401
+from .dense import DenseGB300, batch_hea_tfim, plan  # noqa: F401
 from ._native import KbwgError, build_info, launch_count, load  # noqa: F401

@@ -58,6 +58,8 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, ctypes.c_uint32, _DP, _DP]),
     "kbwg_param_shift_gradient": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_int32), _U,
                                          ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, _DP, _DP]),
+    "kbwg_batch_hea_tfim": (_I32, [_U, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                   _U64P, _DP, _U, _D, _D, _I32, ctypes.c_uint32, _DP]),
     "kbwg_clear": (_I32, [_P]),
     "kbwg_flush": (_I32, [_P]),
     "kbwg_get_state": (_I32, [_P, _P, _U]),

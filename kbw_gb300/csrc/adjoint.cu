@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256) k_inner_re(const cx<T> *__restrict__ a, c
 template <class P> struct Grad;
 
 template <class T>
-struct Grad<Exact<T>> {
+struct Grad<Fast<T>> {
     using Amp = cx<T>;
     using Acc = T;
     static __device__ __forceinline__ Acc zero() { return (T)0; }
@@ -695,13 +695,13 @@ int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::ve
         return KBWG_EUNSUPPORTED;
     }
     if (s.prec == 0)
-        return adjoint_run<Exact<float>, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
-                                                                                  grad_per_gate, max_ckpt);
+        return adjoint_run<Fast<float>, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
+                                                                                 grad_per_gate, max_ckpt);
     if (s.flags & KBWG_FLAG_FAST_C128)
         return adjoint_run<FFPol, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
                                                                              grad_per_gate, max_ckpt);
-    return adjoint_run<Exact<double>, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
-                                                                                 grad_per_gate, max_ckpt);
+    return adjoint_run<Fast<double>, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
+                                                                                grad_per_gate, max_ckpt);
 }
 
 }  // namespace kbwg

@@ -741,6 +741,19 @@ int32_t kbwg_param_shift_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t
     GUARD_END
 }
 
+int32_t kbwg_batch_hea_tfim(uintptr_t n_circuits, const uint32_t *num_qubits, const uint32_t *layers,
+                            const uint64_t *param_offset, const double *params, uintptr_t n_params, double zz,
+                            double x, int32_t precision, uint32_t flags, double *energies) {
+    GUARD_BEGIN
+    if (n_circuits == 0) return KBWG_OK;
+    if (!num_qubits || !layers || !param_offset || !energies || (n_params && !params))
+        return fail(KBWG_EINVAL, "null argument");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    return hea_batch(precision, (flags & KBWG_FLAG_FAST_C128) != 0, n_circuits, num_qubits, layers, param_offset,
+                     params, n_params, zz, x, energies);
+    GUARD_END
+}
+
 int32_t kbwg_clear(kbwg_sim *s) {
     GUARD_BEGIN
     ENTER(s);

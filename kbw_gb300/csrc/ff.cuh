@@ -158,7 +158,7 @@ FFI double to_double(f2 v) {
 }
 
 // Split a binary64 constant on the host (round-to-nearest hi).
-inline f2 split_constant(double c) {
+FFI f2 split_constant(double c) {
     const float h = (float)c;
     return f2{h, (float)(c - (double)h)};
 }

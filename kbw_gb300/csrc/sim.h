@@ -93,6 +93,11 @@ struct PauliString {
 // Gradient types of the adjoint sweep.
 enum { GT_NONE = 0, GT_X = 1, GT_Y = 2, GT_Z = 3, GT_P1 = 4 };
 
+// Batched hardware-efficient-ansatz circuits with ring-TFIM energies (hea.cu).
+int32_t hea_batch(int precision, bool fast_c128, size_t ncirc, const uint32_t *num_qubits, const uint32_t *layers,
+                  const uint64_t *param_offset, const double *params, size_t nparams, double zz, double xc,
+                  double *energies);
+
 // Adjoint gradient (adjoint.cu).  fwd: the circuit; angles: each gate's
 // angle; gtype: GT_* per gate (GT_NONE if not differentiated).  Writes E and
 // dE/dtheta per gate; the handle ends in |0...0>.  Returns 0 or a KBWG_* code.

@@ -227,7 +227,8 @@ static cudaError_t run_fused_t(Sim &s, const GateDesc *gates, size_t count) {
         s.last_passes = count;
         return cudaSuccess;
     }
-    return run_fused_p<Exact<T>, K, R>(s, gates, count);
+    if (s.flags & KBWG_FLAG_EXACT_ORDER) return run_fused_p<Exact<T>, K, R>(s, gates, count);
+    return run_fused_p<Fast<T>, K, R>(s, gates, count);
 }
 
 // Complex128 float-float path: rewrite the queue so that uncontrolled H

@@ -258,6 +258,28 @@ class DenseGB300:
         return int(g.value), int(p.value)
 
 
+def batch_hea_tfim(circuits, zz=1.0, x=0.5, prec="c64", fast_c128=False):
+    """Energies of many hardware-efficient-ansatz circuits in one launch.
+    circuits: list of (num_qubits, layers, params) as circuits.hea_batch()."""
+    lib = N.load()
+    nc = len(circuits)
+    nq = np.ascontiguousarray([c[0] for c in circuits], dtype=np.uint32)
+    ly = np.ascontiguousarray([c[1] for c in circuits], dtype=np.uint32)
+    offs = np.zeros(nc, np.uint64)
+    total = 0
+    for i, c in enumerate(circuits):
+        offs[i] = total
+        total += len(c[2])
+    params = np.ascontiguousarray(np.concatenate([np.asarray(c[2], np.float64) for c in circuits])
+                                  if nc else np.zeros(1), dtype=np.float64)
+    out = np.zeros(max(nc, 1), np.float64)
+    flags = N.FLAG_FAST_C128 if fast_c128 else 0
+    N.check(lib.kbwg_batch_hea_tfim(nc, _p(nq, ctypes.c_uint32), _p(ly, ctypes.c_uint32), _p(offs, ctypes.c_uint64),
+                                    _p(params, ctypes.c_double), int(total), float(zz), float(x), _DT[prec][0],
+                                    flags, _p(out, ctypes.c_double)))
+    return out[:nc]
+
+
 def _gate_array(circuit):
     arr = (N.Gate * max(len(circuit), 1))()
     for i, (kind, t, ctrl, ang) in enumerate(circuit):
