@@ -580,6 +580,8 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
     CUDA_TRY(s->tmp3.ensure((n_strings + 1) * 8));
     double *d_vals = (double *)s->tmp3.ptr;
     size_t i = 0;
+    std::vector<size_t> slot_of;  // group order -> string index
+    slot_of.reserve(n_strings);
     while (i < n_strings) {
         PauliGroup g;
         memset(&g, 0, sizeof g);
@@ -605,12 +607,14 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
             using T = std::remove_pointer_t<decltype(tp)>;
             return launch_pauli_group<T>(s->state, s->n, g, s->rs, s->stream);
         }));
-        for (size_t k = 0; k < idx.size(); k++)
-            CUDA_TRY(cudaMemcpyAsync(d_vals + idx[k], s->rs.result + k, 8, cudaMemcpyDeviceToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(d_vals + slot_of.size(), s->rs.result, idx.size() * 8, cudaMemcpyDeviceToDevice,
+                                 s->stream));
+        slot_of.insert(slot_of.end(), idx.begin(), idx.end());
     }
-    std::vector<double> vals(n_strings + 1);
-    if (n_strings) CUDA_TRY(copy_async(vals.data(), d_vals, n_strings * 8, cudaMemcpyDeviceToHost, s->stream));
+    std::vector<double> grouped(n_strings + 1), vals(n_strings + 1);
+    if (n_strings) CUDA_TRY(copy_async(grouped.data(), d_vals, n_strings * 8, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (size_t j = 0; j < n_strings; j++) vals[slot_of[j]] = grouped[j];
     double total = 0.0;  // sum in string order, as the reference's zip/map/sum
     for (size_t k = 0; k < n_strings; k++) total += vals[k] * strs[k].coef;
     *out = total;

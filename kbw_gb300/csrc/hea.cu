@@ -162,7 +162,10 @@ __device__ uint32_t hea_build(TileGate *sg, uint8_t *stage_layout, uint16_t *sta
             ry.tb = (uint8_t)lb;
             double sn, cs;
             hea_sincos<P>(0.5 * th, &sn, &cs);
-            HeaConst<P>::set(ry, cs, sn, 0.0, 0.0);
+            if constexpr (P::kRot)
+                HeaConst<P>::set(ry, cs, -sn, sn, cs);  // rotation form out0 = c a0 - s a1, out1 = s a0 + c a1
+            else
+                HeaConst<P>::set(ry, cs, sn, 0.0, 0.0);
             TileGate &rz = sg[cnt++];
             memset(&rz, 0, sizeof rz);
             rz.cls = TG_RZ;
@@ -201,6 +204,8 @@ __device__ uint32_t hea_build(TileGate *sg, uint8_t *stage_layout, uint16_t *sta
             stage_end[nstages] = (uint16_t)cnt;
             nstages++;
         }
+        const int R0 = stage_layout[nstages - 1] == LAYOUT_A ? kLaneBits : K - R;
+        for (uint32_t i = start; i < cnt; i++) tile_gate_dispatch(sg[i], R0, R);
     }
     return cnt;
 }

@@ -17,7 +17,7 @@ struct ReduceScratch {
 };
 constexpr int kReduceBlocks = 152 * 4;  // fixed grid: deterministic partition
 constexpr int kReduceThreads = 256;
-constexpr int kMaxTerms = 16;
+constexpr int kMaxTerms = 32;
 
 // Sequential-measurement control block, updated on the device by the last
 // block of each reduction step (kbw src/quantum_execution.rs:272-292).

@@ -159,6 +159,7 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                     else
                         t.co |= 1ull << q;
                 }
+                tile_gate_dispatch(t, layout == LAYOUT_A ? kLaneBits : K - R, R);
                 sw.gates.push_back(t);
                 sw.src.push_back((uint32_t)i);
             }

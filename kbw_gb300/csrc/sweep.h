@@ -39,17 +39,51 @@ enum {
 __host__ __device__ inline bool tg_diagonal(uint32_t cls) { return cls >= TG_Z; }
 constexpr uint8_t TG_OUTER = 0xFF;  // tb value: diagonal gate whose target lies outside the tile
 
-// One gate as a tile sees it (48 bytes; staged in shared memory).
+// Dispatch codes: what a thread does for a gate in its stage's layout.
+enum {
+    OP_LANE = 0,   // + class (X..RY): target on a lane bit, partner by warp shuffle
+    OP_REG = 8,    // + class * 4 + register bit: target on a register bit, in-thread pairs
+    OP_DREG = 32,  // + (class - TG_Z) * 4 + register bit: diagonal, target on a register bit
+    OP_DFIX = 48   // + (class - TG_Z): diagonal, side fixed per thread (lane/warp bit) or per tile
+};
+
+// One gate as a tile sees it (64 bytes; staged in shared memory).  op, rb,
+// fneed and creg are precomputed by the planner for the layout of the stage
+// the gate runs in.
 struct TileGate {
     uint8_t cls;
     uint8_t sub;
     uint8_t tb;    // local target bit, or TG_OUTER
     uint8_t tout;  // global target qubit when tb == TG_OUTER
-    uint32_t cl;   // control mask on local bits
-    uint64_t co;   // control mask on bits outside the tile (global positions)
+    uint8_t op;    // OP_* dispatch code
+    uint8_t rb;    // register bit of the target (when it is one)
+    uint16_t pad0;
+    uint32_t cl;     // control mask on local bits
+    uint32_t fneed;  // controls on this stage's lane/warp bits
+    uint32_t creg;   // controls on this stage's register bits (register-index mask)
+    uint32_t pad1;
+    uint64_t co;     // control mask on bits outside the tile (global positions)
     double c[4];
 };
-static_assert(sizeof(TileGate) == 48, "TileGate layout");
+static_assert(sizeof(TileGate) == 64, "TileGate layout");
+
+// Fill op/rb/fneed/creg of a gate for a stage whose register bits start at
+// local bit R0 (R register bits).
+__host__ __device__ inline void tile_gate_dispatch(TileGate &g, int R0, int R) {
+    const uint32_t regmask = ((1u << R) - 1u) << R0;
+    g.fneed = g.cl & ~regmask;
+    g.creg = (g.cl & regmask) >> R0;
+    const int rb = (int)g.tb - R0;
+    const bool reg_target = g.tb != TG_OUTER && rb >= 0 && rb < R;
+    g.rb = reg_target ? (uint8_t)rb : 0;
+    if (!tg_diagonal(g.cls)) {
+        g.op = (g.tb < kLaneBits) ? (uint8_t)(OP_LANE + g.cls) : (uint8_t)(OP_REG + g.cls * 4 + rb);
+    } else if (g.cls != TG_SCALE && reg_target) {
+        g.op = (uint8_t)(OP_DREG + (g.cls - TG_Z) * 4 + rb);
+    } else {
+        g.op = (uint8_t)(OP_DFIX + (g.cls - TG_Z));
+    }
+}
 
 // Layout A holds local bits [5, 5+R) in registers, layout B [K-R, K).
 enum { LAYOUT_A = 0, LAYOUT_B = 1 };

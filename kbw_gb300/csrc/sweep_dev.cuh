@@ -61,6 +61,7 @@ struct Exact {
     using Amp = cx<T>;
     using Mem = cx<T>;
     using Scalar = T;
+    static constexpr bool kRot = false;  // per-class bodies (see FFPol)
     static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
     // Constants are stored in T on the host (exact: they are T values widened
@@ -177,7 +178,7 @@ struct Fast : Exact<T> {
 // and are rounded back on the way out.  Constants arrive pre-split by
 // pack_host.  Classes used only here: H sub 1 (no 1/sqrt(2): the host folds
 // it into a final scale gate), PI (|1> times i^q, free) and SCALE (every
-// amplitude times c0 + i c1, the folded global factor).
+// amplitude times one complex factor, the folded global factor).
 struct FFPol {
     struct Amp {
         ff::f2 re, im;
@@ -191,10 +192,43 @@ struct FFPol {
         return Amp{ff::from_double(a.re), ff::from_double(a.im)};
     }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return Mem{ff::to_double(a.re), ff::to_double(a.im)}; }
+    // One body for every real-coefficient rotation (code size: the per-class
+    // float-float bodies overflow the instruction cache).  H, RX and RY
+    // become ROT: out0 = c0 a0 + c1 M(a1), out1 = c2 M(a0) + c3 a1 with
+    // M = -i for RX (sub 1) and the identity otherwise.  P and SCALE keep
+    // their factor in (c2, c3), the |1> slot of RZ, so P, RZ and SCALE share
+    // one multiply body.
+    static constexpr bool kRot = true;
     static void pack_host(TileGate &g) {
+        double c[4] = {g.c[0], g.c[1], g.c[2], g.c[3]};
+        bool rot = true;
+        uint8_t m = 0;
+        if (g.cls == TG_H) {
+            const double h = g.sub ? 1.0 : c[0];
+            c[0] = c[1] = c[2] = h;
+            c[3] = -h;
+        } else if (g.cls == TG_RY) {
+            const double cs = c[0], sn = c[1];
+            c[0] = cs, c[1] = -sn, c[2] = sn, c[3] = cs;
+        } else if (g.cls == TG_RX) {
+            const double cs = c[0], sn = c[1];
+            c[0] = cs, c[1] = sn, c[2] = sn, c[3] = cs;
+            m = 1;
+        } else {
+            rot = false;
+            if (g.cls == TG_P || g.cls == TG_SCALE) {
+                c[2] = c[0], c[3] = c[1];
+                c[0] = 1.0, c[1] = 0.0;
+            }
+        }
+        if (rot) {
+            g.cls = TG_RY;
+            g.sub = m;
+            g.op = (g.op < OP_REG) ? (uint8_t)(OP_LANE + TG_RY) : (uint8_t)(OP_REG + TG_RY * 4 + g.rb);
+        }
         float f[8];
         for (int i = 0; i < 4; i++) {
-            const ff::f2 v = ff::split_constant(g.c[i]);
+            const ff::f2 v = ff::split_constant(c[i]);
             f[2 * i] = v.h;
             f[2 * i + 1] = v.l;
         }
@@ -264,6 +298,19 @@ struct FFPol {
     static __device__ __forceinline__ Amp cmul(Amp a, ff::f2 c, ff::f2 s) {
         return Amp{ff::dot2(c, a.re, ff::neg(s), a.im), ff::dot2(c, a.im, s, a.re)};
     }
+    static __device__ __forceinline__ Amp mflag(Amp a, bool m) { return m ? Amp{a.im, ff::neg(a.re)} : a; }
+    static __device__ __forceinline__ void rot_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
+        const Amp m1 = mflag(a1, sub != 0), m0 = mflag(a0, sub != 0);
+        const Amp n0{ff::dot2(k.c0, a0.re, k.c1, m1.re), ff::dot2(k.c0, a0.im, k.c1, m1.im)};
+        const Amp n1{ff::dot2(k.c2, m0.re, k.c3, a1.re), ff::dot2(k.c2, m0.im, k.c3, a1.im)};
+        a0 = n0;
+        a1 = n1;
+    }
+    // lane form: out = A self + B M(o), (A, B) = (c0, c1) on |0>, (c3, c2) on |1>
+    static __device__ __forceinline__ Amp rot_half(ff::f2 A, ff::f2 B, bool m, Amp self, Amp o) {
+        const Amp mo = mflag(o, m);
+        return Amp{ff::dot2(A, self.re, B, mo.re), ff::dot2(A, self.im, B, mo.im)};
+    }
     static __device__ __forceinline__ Amp pi_mul(Amp a, int q) {
         if (q == 1) return Amp{ff::neg(a.im), a.re};
         if (q == 2) return Amp{ff::neg(a.re), ff::neg(a.im)};
@@ -289,9 +336,13 @@ __device__ __forceinline__ void reg_pairs(typename P::Amp (&v)[1 << R], int sub,
                 v[j1] = t;
             }
             if (CLS == TG_Y) P::y_pair(v[j0], v[j1]);
-            if (CLS == TG_H) P::h_pair(sub, k, v[j0], v[j1]);
-            if (CLS == TG_RX) P::rx_pair(k, v[j0], v[j1]);
-            if (CLS == TG_RY) P::ry_pair(k, v[j0], v[j1]);
+            if constexpr (P::kRot) {
+                if (CLS == TG_RY) P::rot_pair(sub, k, v[j0], v[j1]);
+            } else {
+                if (CLS == TG_H) P::h_pair(sub, k, v[j0], v[j1]);
+                if (CLS == TG_RX) P::rx_pair(k, v[j0], v[j1]);
+                if (CLS == TG_RY) P::ry_pair(k, v[j0], v[j1]);
+            }
         }
     }
 }
@@ -318,6 +369,32 @@ template <class P, int R, int B>
 __device__ __forceinline__ void diag_reg(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
                                          uint32_t creg) {
     constexpr int NR = 1 << R;
+    if constexpr (P::kRot) {
+        if (cls == TG_Z) {
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if ((j >> B) & 1)
+                    if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
+        } else if (cls == TG_PI) {
+            const int q = (int)reinterpret_cast<const float &>(k.c0);
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if ((j >> B) & 1)
+                    if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
+        } else {
+            if (cls == TG_RZ) {
+#pragma unroll
+                for (int j = 0; j < NR; j++)
+                    if (!((j >> B) & 1))
+                        if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
+            }
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if ((j >> B) & 1)
+                    if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c2, k.c3);
+        }
+        return;
+    }
     switch (cls) {
     case TG_Z:
 #pragma unroll
@@ -353,6 +430,27 @@ template <class P, int R>
 __device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
                                            uint32_t creg, bool one) {
     constexpr int NR = 1 << R;
+    if constexpr (P::kRot) {
+        if (cls == TG_SCALE) one = true;
+        if (!one && cls != TG_RZ) return;
+        if (cls == TG_Z) {
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
+        } else if (cls == TG_PI) {
+            const int q = (int)reinterpret_cast<const float &>(k.c0);
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
+        } else {
+            const auto c = one ? k.c2 : k.c0;
+            const auto s = one ? k.c3 : k.c1;
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+                if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], c, s);
+        }
+        return;
+    }
     if (cls == TG_SCALE) {
 #pragma unroll
         for (int j = 0; j < NR; j++)
@@ -384,46 +482,92 @@ __device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], int cls
     }
 }
 
+template <class P, int R, int B>
+__device__ __forceinline__ void reg_dispatch(typename P::Amp (&v)[1 << R], int cls, int sub,
+                                             const typename P::K4 &k, uint32_t creg) {
+    if constexpr (B < R && P::kRot) {
+        switch (cls) {
+        case TG_X: reg_pairs<P, R, B, TG_X>(v, sub, k, creg); break;
+        case TG_Y: reg_pairs<P, R, B, TG_Y>(v, sub, k, creg); break;
+        default: reg_pairs<P, R, B, TG_RY>(v, sub, k, creg); break;
+        }
+    } else if constexpr (B < R) {
+        switch (cls) {
+        case TG_X: reg_pairs<P, R, B, TG_X>(v, sub, k, creg); break;
+        case TG_Y: reg_pairs<P, R, B, TG_Y>(v, sub, k, creg); break;
+        case TG_H: reg_pairs<P, R, B, TG_H>(v, sub, k, creg); break;
+        case TG_RX: reg_pairs<P, R, B, TG_RX>(v, sub, k, creg); break;
+        default: reg_pairs<P, R, B, TG_RY>(v, sub, k, creg); break;
+        }
+    }
+}
+
+template <class P, int R, int B>
+__device__ __forceinline__ void dreg_dispatch(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
+                                              uint32_t creg) {
+    if constexpr (B < R) diag_reg<P, R, B>(v, cls, k, creg);
+}
+
 // Apply one gate to the thread's registers.  F = the thread's fixed local
-// bits (lane and warp), R0 = first local bit held in registers.
+// bits (lane and warp).  The gate's op/rb/fneed/creg were computed by the
+// planner for the layout this stage runs in.
 template <class P, int K, int R>
-__device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int R0, uint32_t F,
+__device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int /*R0*/, uint32_t F,
                                           uint64_t base) {
-    static_assert(R >= 3 && R <= 5, "register bits 0..4");
+    static_assert(R >= 3 && R <= 4, "dispatch covers register bits 0..3");
     constexpr int NR = 1 << R;
     if ((base & g.co) != g.co) return;  // a control outside the tile is 0 for the whole tile
-    const uint32_t regmask = (uint32_t)(NR - 1) << R0;
-    const uint32_t fixed_need = g.cl & ~regmask;
-    const bool fok = (F & fixed_need) == fixed_need;  // controls on this thread's lane/warp bits
-    const uint32_t tb = g.tb;
-    const uint32_t cls = g.cls;
-    const bool lane_target = !tg_diagonal(cls) && tb < (uint32_t)kLaneBits;
-    // Threads whose lane/warp controls are 0 leave, except for lane-bit
-    // targets: there every lane must take part in the warp shuffle.
-    if (!fok && !lane_target) return;
-    const typename P::K4 k = P::load(g);
-    const uint32_t creg = (g.cl & regmask) >> R0;
-    if (lane_target) {
-        // partner in lane F ^ (1 << tb); a control never sits on the target
-        // bit, so both halves of a pair see the same control values
+    const bool fok = (F & g.fneed) == g.fneed;
+    const uint32_t op = g.op;
+    const uint32_t creg = g.creg;
+    if (op < OP_REG) {
+        // lane-bit target: every lane takes part in the shuffle (a control is
+        // never the target, so both halves of a pair share control values)
+        const typename P::K4 k = P::load(g);
+        const uint32_t tb = g.tb;
         const bool one = ((F >> tb) & 1u) != 0;
         const int m = 1 << tb;
-        switch (cls) {
-        case TG_X:
+        if constexpr (P::kRot) {
+            if (op == OP_LANE + TG_X) {
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const typename P::Amp o = P::shfl(v[j], m);
+                    if (fok && KBWG_CTRL_OK(j)) v[j] = o;
+                }
+            } else if (op == OP_LANE + TG_Y) {
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const typename P::Amp o = P::shfl(v[j], m);
+                    if (fok && KBWG_CTRL_OK(j)) v[j] = P::y_half(o, one);
+                }
+            } else {
+                const auto A = one ? k.c3 : k.c0;
+                const auto Bc = one ? k.c2 : k.c1;
+                const bool mm = g.sub != 0;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const typename P::Amp o = P::shfl(v[j], m);
+                    if (fok && KBWG_CTRL_OK(j)) v[j] = P::rot_half(A, Bc, mm, v[j], o);
+                }
+            }
+            return;
+        } else {
+        switch (op) {
+        case OP_LANE + TG_X:
 #pragma unroll
             for (int j = 0; j < NR; j++) {
                 const typename P::Amp o = P::shfl(v[j], m);
                 if (fok && KBWG_CTRL_OK(j)) v[j] = o;
             }
             break;
-        case TG_Y:
+        case OP_LANE + TG_Y:
 #pragma unroll
             for (int j = 0; j < NR; j++) {
                 const typename P::Amp o = P::shfl(v[j], m);
                 if (fok && KBWG_CTRL_OK(j)) v[j] = P::y_half(o, one);
             }
             break;
-        case TG_H: {
+        case OP_LANE + TG_H: {
             const auto sg = P::sign(one);
 #pragma unroll
             for (int j = 0; j < NR; j++) {
@@ -432,14 +576,14 @@ __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v
             }
             break;
         }
-        case TG_RX:
+        case OP_LANE + TG_RX:
 #pragma unroll
             for (int j = 0; j < NR; j++) {
                 const typename P::Amp o = P::shfl(v[j], m);
                 if (fok && KBWG_CTRL_OK(j)) v[j] = P::rx_half(k, v[j], o);
             }
             break;
-        default: {  // TG_RY
+        default: {
             const auto ss = P::signed_s(k, one);
 #pragma unroll
             for (int j = 0; j < NR; j++) {
@@ -450,37 +594,35 @@ __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v
         }
         }
         return;
+        }
     }
-    if (tg_diagonal(cls)) {
-        const int rb = (int)tb - R0;
-        if (cls != TG_SCALE && tb != TG_OUTER && rb >= 0 && rb < R) {
-            switch (rb) {
-            case 0: diag_reg<P, R, 0>(v, cls, k, creg); break;
-            case 1: diag_reg<P, R, 1>(v, cls, k, creg); break;
-            case 2: diag_reg<P, R, 2>(v, cls, k, creg); break;
-            case 3:
-                if constexpr (R > 3) diag_reg<P, R, (R > 3 ? 3 : 0)>(v, cls, k, creg);
-                break;
-            default:
-                if constexpr (R > 4) diag_reg<P, R, (R > 4 ? 4 : 0)>(v, cls, k, creg);
-                break;
-            }
-        } else {
-            const bool one = (cls == TG_SCALE) ? true
-                             : (tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0)
-                                                : (((F >> tb) & 1u) != 0);
-            diag_fixed<P, R>(v, cls, k, creg, one);
+    if (!fok) return;
+    const typename P::K4 k = P::load(g);
+    if (op < OP_DREG) {
+        const int c = (int)(op - OP_REG) >> 2;
+        switch ((op - OP_REG) & 3u) {
+        case 0: reg_dispatch<P, R, 0>(v, c, g.sub, k, creg); break;
+        case 1: reg_dispatch<P, R, 1>(v, c, g.sub, k, creg); break;
+        case 2: reg_dispatch<P, R, 2>(v, c, g.sub, k, creg); break;
+        default: reg_dispatch<P, R, 3>(v, c, g.sub, k, creg); break;
         }
         return;
     }
-    const int b = (int)tb - R0;
-    switch (cls) {
-    case TG_X: reg_gate<P, R, TG_X>(v, g.sub, k, b, creg); break;
-    case TG_Y: reg_gate<P, R, TG_Y>(v, g.sub, k, b, creg); break;
-    case TG_H: reg_gate<P, R, TG_H>(v, g.sub, k, b, creg); break;
-    case TG_RX: reg_gate<P, R, TG_RX>(v, g.sub, k, b, creg); break;
-    default: reg_gate<P, R, TG_RY>(v, g.sub, k, b, creg); break;
+    if (op < OP_DFIX) {
+        const int c = TG_Z + ((int)(op - OP_DREG) >> 2);
+        switch ((op - OP_DREG) & 3u) {
+        case 0: dreg_dispatch<P, R, 0>(v, c, k, creg); break;
+        case 1: dreg_dispatch<P, R, 1>(v, c, k, creg); break;
+        case 2: dreg_dispatch<P, R, 2>(v, c, k, creg); break;
+        default: dreg_dispatch<P, R, 3>(v, c, k, creg); break;
+        }
+        return;
     }
+    const int c = TG_Z + (int)(op - OP_DFIX);
+    const bool one = (c == TG_SCALE) ? true
+                     : (g.tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0)
+                                          : (((F >> g.tb) & 1u) != 0);
+    diag_fixed<P, R>(v, c, k, creg, one);
 }
 
 #undef KBWG_CTRL_OK
