@@ -647,11 +647,12 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
 
     // 1. forward from |0>
     s.queue.clear();
-    e = launch_init<T>(s.state, s.n, s.stream);
+    e = init_state(s);
     if (e != cudaSuccess) return fail_cuda(e, "init");
     for (size_t seg = 0; seg < S; seg++) {
         s.queue.assign(fwd.begin() + b[seg], fwd.begin() + b[seg + 1]);
         e = flush_queue(s);
+        if (e == cudaSuccess) e = ensure_binary64(s);  // checkpoints and the reverse sweeps use binary64
         if (e != cudaSuccess) return fail_cuda(e, "forward");
         if (seg + 1 < S) {
             e = cudaMemcpyAsync(bufs.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
@@ -680,7 +681,7 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         if (e != cudaSuccess) return fail_cuda(e, "gradient read-back");
     }
     // leave the handle in |0...0>
-    e = launch_init<T>(s.state, s.n, s.stream);
+    e = init_state(s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) return fail_cuda(e, "finish");
     bufs.release();

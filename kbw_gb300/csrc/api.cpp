@@ -125,6 +125,14 @@ static cudaError_t flush_t(Sim &s) {
 
 cudaError_t flush_queue(Sim &s) { return s.prec ? flush_t<double>(s) : flush_t<float>(s); }
 
+// Flush, then bring a float-float resident state back to binary64: every
+// operation other than gate application and qubit swaps reads binary64.
+static cudaError_t settle(Sim &s) {
+    cudaError_t e = flush_queue(s);
+    if (e != cudaSuccess) return e;
+    return ensure_binary64(s);
+}
+
 }  // namespace kbwg
 
 using namespace kbwg;
@@ -221,7 +229,7 @@ int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_s
     char *end = nullptr;
     unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
     s->rng = (seed && end && *end == 0 && *seed) ? (uint64_t)sv : (uint64_t)(uintptr_t)s ^ 0x5DEECE66Dull;
-    e = s->prec ? launch_init<double>(s->state, s->n, s->stream) : launch_init<float>(s->state, s->n, s->stream);
+    e = init_state(*s);
     if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
     e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
@@ -331,7 +339,7 @@ int32_t kbwg_measure_p1(kbwg_sim *s, uintptr_t target, double *p1) {
     ENTER(s);
     if (!p1) return fail(KBWG_EINVAL, "null output");
     if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     const uint64_t bit = 1ull << target;
     CUDA_TRY(dispatch(s, [&](auto *tp) {
         using T = std::remove_pointer_t<decltype(tp)>;
@@ -348,7 +356,7 @@ int32_t kbwg_measure_collapse(kbwg_sim *s, uintptr_t target, bool result, double
     GUARD_BEGIN
     ENTER(s);
     if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     const uint64_t bit = 1ull << target;
     CUDA_TRY(dispatch(s, [&](auto *tp) {
         using T = std::remove_pointer_t<decltype(tp)>;
@@ -373,7 +381,7 @@ int32_t kbwg_measure(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, c
     }
     *result = 0;
     if (n_qubits == 0) return KBWG_OK;
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     MeasureCtl &c = *s->h_ctl;
     memset(&c, 0, sizeof c);
     c.scale2 = 1.0;
@@ -405,7 +413,7 @@ int32_t kbwg_dump(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, uint
     if (n_qubits > 64) return fail(KBWG_EINVAL, "more than 64 qubits");
     for (uintptr_t i = 0; i < n_qubits; i++)
         if (qubits[i] >= s->n) return fail(KBWG_EINVAL, "qubit out of range");
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     const int B = dump_blocks(s->n);
     CUDA_TRY(s->tmp0.ensure((size_t)B * 8));
     uint64_t *d_counts = (uint64_t *)s->tmp0.ptr;
@@ -465,7 +473,7 @@ int32_t kbwg_sample(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, ui
         set_error(KBWG_ECAPACITY, "sample capacity too small");
         return KBWG_ECAPACITY;
     }
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     const int B = sample_blocks(s->n);
     CUDA_TRY(s->tmp0.ensure((size_t)B * 8));
     double *d_bs = (double *)s->tmp0.ptr;
@@ -663,7 +671,7 @@ int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubi
     std::vector<PauliString> strs;
     int32_t r = parse_hamiltonian(s->n, paulis, qubits, offsets, coefficients, n_strings, strs);
     if (r) return r;
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     return exp_value_core(s, strs, out);
     GUARD_END
 }
@@ -683,7 +691,7 @@ int32_t kbwg_adjoint_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_g
     std::vector<int> gtype;
     r = parse_grad_circuit(s, gates, n_gates, param_index, n_params, fwd, angles, gtype);
     if (r) return r;
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     std::vector<double> per_gate;
     r = adjoint_gradient(*s, fwd, angles, gtype, strs, energy, per_gate, max_checkpoints);
     if (r) return r;
@@ -716,12 +724,9 @@ int32_t kbwg_param_shift_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t
     // (src/quantum_execution.rs:392-405)
     auto evaluate = [&](const std::vector<GateDesc> &circ, double *e) -> int32_t {
         s->queue.clear();
-        CUDA_TRY(dispatch(s, [&](auto *tp) {
-            using T = std::remove_pointer_t<decltype(tp)>;
-            return launch_init<T>(s->state, s->n, s->stream);
-        }));
+        CUDA_TRY(init_state(*s));
         s->queue = circ;
-        CUDA_TRY(flush_queue(*s));
+        CUDA_TRY(settle(*s));
         return exp_value_core(s, strs, e);
     };
     r = evaluate(fwd, energy);
@@ -762,10 +767,7 @@ int32_t kbwg_clear(kbwg_sim *s) {
     GUARD_BEGIN
     ENTER(s);
     s->queue.clear();
-    CUDA_TRY(dispatch(s, [&](auto *tp) {
-        using T = std::remove_pointer_t<decltype(tp)>;
-        return launch_init<T>(s->state, s->n, s->stream);
-    }));
+    CUDA_TRY(init_state(*s));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return KBWG_OK;
     GUARD_END
@@ -775,7 +777,7 @@ int32_t kbwg_get_state(kbwg_sim *s, void *host_dst, uintptr_t bytes) {
     GUARD_BEGIN
     ENTER(s);
     if (!host_dst || bytes != s->ns * s->elem) return fail(KBWG_EINVAL, "buffer size must equal 2^n * element size");
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     CUDA_TRY(copy_async(host_dst, s->state, bytes, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return check_device_error(s);
@@ -787,6 +789,7 @@ int32_t kbwg_set_state(kbwg_sim *s, const void *host_src, uintptr_t bytes) {
     ENTER(s);
     if (!host_src || bytes != s->ns * s->elem) return fail(KBWG_EINVAL, "buffer size must equal 2^n * element size");
     s->queue.clear();
+    s->ff_resident = false;
     CUDA_TRY(copy_async(s->state, host_src, bytes, cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return KBWG_OK;
@@ -797,7 +800,7 @@ int32_t kbwg_state_info(kbwg_sim *s, uintptr_t *num_qubits, int32_t *precision, 
                         uintptr_t *bytes) {
     GUARD_BEGIN
     ENTER(s);
-    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(settle(*s));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     if (num_qubits) *num_qubits = s->n;
     if (precision) *precision = s->prec;
@@ -906,8 +909,8 @@ int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative) {
     if (a->n != b->n || a->prec != b->prec || a->device != b->device)
         return fail(KBWG_EINVAL, "handles differ in size, precision or device");
     ENTER(a);
-    CUDA_TRY(flush_queue(*a));
-    CUDA_TRY(flush_queue(*b));
+    CUDA_TRY(settle(*a));
+    CUDA_TRY(settle(*b));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(dispatch(a, [&](auto *tp) {
         using T = std::remove_pointer_t<decltype(tp)>;

@@ -162,10 +162,7 @@ __device__ uint32_t hea_build(TileGate *sg, uint8_t *stage_layout, uint16_t *sta
             ry.tb = (uint8_t)lb;
             double sn, cs;
             hea_sincos<P>(0.5 * th, &sn, &cs);
-            if constexpr (P::kRot)
-                HeaConst<P>::set(ry, cs, -sn, sn, cs);  // rotation form out0 = c a0 - s a1, out1 = s a0 + c a1
-            else
-                HeaConst<P>::set(ry, cs, sn, 0.0, 0.0);
+            HeaConst<P>::set(ry, cs, sn, 0.0, 0.0);
             TileGate &rz = sg[cnt++];
             memset(&rz, 0, sizeof rz);
             rz.cls = TG_RZ;

@@ -1,6 +1,7 @@
 // Unfused kernels: one gate per pass, state initialisation and the
 // qubit-exchange permutation.  The fused tile sweeps live in sweep.cu.
 #include "common.cuh"
+#include "ff.cuh"
 #include "kernels.h"
 
 namespace kbwg {
@@ -43,6 +44,29 @@ __global__ void __launch_bounds__(256) k_init_zero_state(cx<T> *__restrict__ st,
     }
 }
 
+// |0...0> as float-float pairs: amplitude 0 is (hi 1, lo 0, 0, 0); zero
+// amplitudes have the same all-zero bytes in both formats.
+__global__ void __launch_bounds__(256) k_init_zero_state_ff(float4 *__restrict__ st, uint64_t ns) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride)
+        st[s] = make_float4(s == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+}
+
+// binary64 <-> float-float, in place (each thread rewrites its own 16 bytes).
+__global__ void __launch_bounds__(256) k_ff_convert(cx<double> *__restrict__ st, uint64_t ns, int to_ff) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        if (to_ff) {
+            const cx<double> a = st[s];
+            const ff::f2 re = ff::from_double(a.re), im = ff::from_double(a.im);
+            reinterpret_cast<float4 *>(st)[s] = make_float4(re.h, re.l, im.h, im.l);
+        } else {
+            const float4 f = reinterpret_cast<const float4 *>(st)[s];
+            st[s] = cx<double>{ff::to_double(ff::f2{f.x, f.y}), ff::to_double(ff::f2{f.z, f.w})};
+        }
+    }
+}
+
 // In-place exchange of physical qubits a < b: amplitudes with (bit a, bit b)
 // = (1, 0) and (0, 1) trade places; the others stay.  One thread per swapped
 // pair; 2^(n-2) pairs.
@@ -82,6 +106,20 @@ template <class T>
 cudaError_t launch_init(void *st, uint32_t n, cudaStream_t s) {
     const uint64_t ns = 1ull << n;
     k_init_zero_state<T><<<grid_for(ns, 256, 152 * 16), 256, 0, s>>>((cx<T> *)st, ns);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_ff(void *st, uint32_t n, cudaStream_t s) {
+    const uint64_t ns = 1ull << n;
+    k_init_zero_state_ff<<<grid_for(ns, 256, 152 * 16), 256, 0, s>>>((float4 *)st, ns);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ff_convert(void *st, uint32_t n, bool to_ff, cudaStream_t s) {
+    const uint64_t ns = 1ull << n;
+    k_ff_convert<<<grid_for(ns, 256, 152 * 16), 256, 0, s>>>((cx<double> *)st, ns, to_ff ? 1 : 0);
     count_launch();
     return cudaGetLastError();
 }

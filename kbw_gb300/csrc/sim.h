@@ -51,6 +51,9 @@ struct Sim {
     size_t elem = 0;
     void *state = nullptr;
     cudaStream_t stream = nullptr;
+    // complex128 fast path: the buffer holds float-float pairs (hi, lo of the
+    // real part, then of the imaginary part) instead of binary64 while true
+    bool ff_resident = false;
 
     std::vector<GateDesc> queue;  // gates waiting for the next flush
 
@@ -70,6 +73,14 @@ struct Sim {
     uint64_t last_passes = 0;
     uint64_t last_gates = 0;
 };
+
+// True when the handle's gates run in float-float arithmetic with the
+// state kept in float-float form between sweeps.
+bool ff_capable(const Sim &s);
+// Turn a float-float resident state back into binary64 (no-op otherwise).
+cudaError_t ensure_binary64(Sim &s);
+// |0...0> in the handle's resident format.
+cudaError_t init_state(Sim &s);
 
 // Build the descriptor of one trait gate: constants computed in the state
 // precision exactly as kbw Dense<F> does (src/dense.rs:211-334).

@@ -294,10 +294,36 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
     return out;
 }
 
+bool ff_capable(const Sim &s) {
+    return s.prec && (s.flags & KBWG_FLAG_FAST_C128) && s.n >= (uint32_t)TileCfg<double>::K;
+}
+
+cudaError_t ensure_binary64(Sim &s) {
+    if (!s.ff_resident) return cudaSuccess;
+    s.ff_resident = false;
+    return launch_ff_convert(s.state, s.n, false, s.stream);
+}
+
+cudaError_t init_state(Sim &s) {
+    if (ff_capable(s)) {
+        s.ff_resident = true;
+        return launch_init_ff(s.state, s.n, s.stream);
+    }
+    s.ff_resident = false;
+    return s.prec ? launch_init<double>(s.state, s.n, s.stream) : launch_init<float>(s.state, s.n, s.stream);
+}
+
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
-    if (s.prec && (s.flags & KBWG_FLAG_FAST_C128) && s.n >= (uint32_t)TileCfg<double>::K) {
+    if (ff_capable(s)) {
+        // float-float sweeps read and write the float-float form; the state
+        // stays in it until an operation needs binary64
+        if (!s.ff_resident) {
+            cudaError_t e = launch_ff_convert(s.state, s.n, true, s.stream);
+            if (e != cudaSuccess) return e;
+            s.ff_resident = true;
+        }
         std::vector<GateDesc> g = ff_rewrite(gates, count);
-        return run_fused_p<FFPol, TileCfg<double>::K, TileCfg<double>::R>(s, g.data(), g.size());
+        return run_fused_p<FFRes, TileCfg<double>::K, TileCfg<double>::R>(s, g.data(), g.size());
     }
     return s.prec ? run_fused_t<double>(s, gates, count) : run_fused_t<float>(s, gates, count);
 }

@@ -47,42 +47,43 @@ enum {
     OP_DFIX = 48   // + (class - TG_Z): diagonal, side fixed per thread (lane/warp bit) or per tile
 };
 
-// One gate as a tile sees it (64 bytes; staged in shared memory).  op, rb,
-// fneed and creg are precomputed by the planner for the layout of the stage
+// One gate as a tile sees it (64 bytes; staged in shared memory).  The
+// first 16 bytes are the dispatch header a thread reads with one load; op,
+// jm and fneed are precomputed by the planner for the layout of the stage
 // the gate runs in.
-struct TileGate {
-    uint8_t cls;
+struct alignas(16) TileGate {
+    uint8_t op;      // OP_* dispatch code
     uint8_t sub;
-    uint8_t tb;    // local target bit, or TG_OUTER
-    uint8_t tout;  // global target qubit when tb == TG_OUTER
-    uint8_t op;    // OP_* dispatch code
-    uint8_t rb;    // register bit of the target (when it is one)
-    uint16_t pad0;
-    uint32_t cl;     // control mask on local bits
+    uint8_t tb;      // local target bit, or TG_OUTER
+    uint8_t tout;    // global target qubit when tb == TG_OUTER
+    uint16_t jm;     // bit j: register j passes the controls on register bits
+    uint8_t cls;
+    uint8_t rb;      // register bit of the target (when it is one)
     uint32_t fneed;  // controls on this stage's lane/warp bits
-    uint32_t creg;   // controls on this stage's register bits (register-index mask)
-    uint32_t pad1;
+    uint32_t cl;     // control mask on local bits
     uint64_t co;     // control mask on bits outside the tile (global positions)
+    uint32_t creg;   // controls on this stage's register bits (register-index mask)
+    uint32_t pad;
     double c[4];
 };
 static_assert(sizeof(TileGate) == 64, "TileGate layout");
 
-// Fill op/rb/fneed/creg of a gate for a stage whose register bits start at
-// local bit R0 (R register bits).
+// Fill op/rb/jm/fneed/creg of a gate for a stage whose register bits start
+// at local bit R0 (R register bits, R <= 4).
 __host__ __device__ inline void tile_gate_dispatch(TileGate &g, int R0, int R) {
     const uint32_t regmask = ((1u << R) - 1u) << R0;
     g.fneed = g.cl & ~regmask;
     g.creg = (g.cl & regmask) >> R0;
+    uint32_t jm = 0;
+    for (uint32_t j = 0; j < (1u << R); j++)
+        if ((j & g.creg) == g.creg) jm |= 1u << j;
+    g.jm = (uint16_t)jm;
     const int rb = (int)g.tb - R0;
     const bool reg_target = g.tb != TG_OUTER && rb >= 0 && rb < R;
     g.rb = reg_target ? (uint8_t)rb : 0;
-    if (!tg_diagonal(g.cls)) {
-        g.op = (g.tb < kLaneBits) ? (uint8_t)(OP_LANE + g.cls) : (uint8_t)(OP_REG + g.cls * 4 + rb);
-    } else if (g.cls != TG_SCALE && reg_target) {
-        g.op = (uint8_t)(OP_DREG + (g.cls - TG_Z) * 4 + rb);
-    } else {
-        g.op = (uint8_t)(OP_DFIX + (g.cls - TG_Z));
-    }
+    if (!tg_diagonal(g.cls)) g.op = (g.tb < kLaneBits) ? OP_LANE + g.cls : OP_REG + g.cls * 4 + rb;
+    else if (g.cls != TG_SCALE && reg_target) g.op = OP_DREG + (g.cls - TG_Z) * 4 + rb;
+    else g.op = OP_DFIX + (g.cls - TG_Z);
 }
 
 // Layout A holds local bits [5, 5+R) in registers, layout B [K-R, K).

@@ -61,7 +61,6 @@ struct Exact {
     using Amp = cx<T>;
     using Mem = cx<T>;
     using Scalar = T;
-    static constexpr bool kRot = false;  // per-class bodies (see FFPol)
     static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
     // Constants are stored in T on the host (exact: they are T values widened
@@ -192,40 +191,8 @@ struct FFPol {
         return Amp{ff::from_double(a.re), ff::from_double(a.im)};
     }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return Mem{ff::to_double(a.re), ff::to_double(a.im)}; }
-    // One body for every real-coefficient rotation (code size: the per-class
-    // float-float bodies overflow the instruction cache).  H, RX and RY
-    // become ROT: out0 = c0 a0 + c1 M(a1), out1 = c2 M(a0) + c3 a1 with
-    // M = -i for RX (sub 1) and the identity otherwise.  P and SCALE keep
-    // their factor in (c2, c3), the |1> slot of RZ, so P, RZ and SCALE share
-    // one multiply body.
-    static constexpr bool kRot = true;
     static void pack_host(TileGate &g) {
         double c[4] = {g.c[0], g.c[1], g.c[2], g.c[3]};
-        bool rot = true;
-        uint8_t m = 0;
-        if (g.cls == TG_H) {
-            const double h = g.sub ? 1.0 : c[0];
-            c[0] = c[1] = c[2] = h;
-            c[3] = -h;
-        } else if (g.cls == TG_RY) {
-            const double cs = c[0], sn = c[1];
-            c[0] = cs, c[1] = -sn, c[2] = sn, c[3] = cs;
-        } else if (g.cls == TG_RX) {
-            const double cs = c[0], sn = c[1];
-            c[0] = cs, c[1] = sn, c[2] = sn, c[3] = cs;
-            m = 1;
-        } else {
-            rot = false;
-            if (g.cls == TG_P || g.cls == TG_SCALE) {
-                c[2] = c[0], c[3] = c[1];
-                c[0] = 1.0, c[1] = 0.0;
-            }
-        }
-        if (rot) {
-            g.cls = TG_RY;
-            g.sub = m;
-            g.op = (g.op < OP_REG) ? (uint8_t)(OP_LANE + TG_RY) : (uint8_t)(OP_REG + TG_RY * 4 + g.rb);
-        }
         float f[8];
         for (int i = 0; i < 4; i++) {
             const ff::f2 v = ff::split_constant(c[i]);
@@ -298,19 +265,6 @@ struct FFPol {
     static __device__ __forceinline__ Amp cmul(Amp a, ff::f2 c, ff::f2 s) {
         return Amp{ff::dot2(c, a.re, ff::neg(s), a.im), ff::dot2(c, a.im, s, a.re)};
     }
-    static __device__ __forceinline__ Amp mflag(Amp a, bool m) { return m ? Amp{a.im, ff::neg(a.re)} : a; }
-    static __device__ __forceinline__ void rot_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
-        const Amp m1 = mflag(a1, sub != 0), m0 = mflag(a0, sub != 0);
-        const Amp n0{ff::dot2(k.c0, a0.re, k.c1, m1.re), ff::dot2(k.c0, a0.im, k.c1, m1.im)};
-        const Amp n1{ff::dot2(k.c2, m0.re, k.c3, a1.re), ff::dot2(k.c2, m0.im, k.c3, a1.im)};
-        a0 = n0;
-        a1 = n1;
-    }
-    // lane form: out = A self + B M(o), (A, B) = (c0, c1) on |0>, (c3, c2) on |1>
-    static __device__ __forceinline__ Amp rot_half(ff::f2 A, ff::f2 B, bool m, Amp self, Amp o) {
-        const Amp mo = mflag(o, m);
-        return Amp{ff::dot2(A, self.re, B, mo.re), ff::dot2(A, self.im, B, mo.im)};
-    }
     static __device__ __forceinline__ Amp pi_mul(Amp a, int q) {
         if (q == 1) return Amp{ff::neg(a.im), a.re};
         if (q == 2) return Amp{ff::neg(a.re), ff::neg(a.im)};
@@ -318,313 +272,196 @@ struct FFPol {
     }
 };
 
-// ---- per-gate register code -------------------------------------------------------
-#define KBWG_CTRL_OK(j) (creg == 0u || ((uint32_t)(j) & creg) == creg)
+// Float-float policy with the state resident in float-float form in HBM
+// (per amplitude: hi, lo of the real part, then hi, lo of the imaginary
+// part; 16 bytes like binary64): sweeps load and store it unconverted.
+struct FFRes : FFPol {
+    using Mem = FFPol::Amp;
+    static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
+    static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
+};
 
-// Gate on register bit B: 2^(R-1) in-thread pairs.
+// ---- per-gate register code -------------------------------------------------------
+// jm bit j: register j passes the gate's controls on register bits (from the
+// planner), so a controlled gate costs one predicate per register.
+#define KBWG_JM(j) (((jm >> (j)) & 1u) != 0u)
+
+// Gate on register bit B: 2^(R-1) in-thread pairs (a control is never the
+// target, so both halves of a pair share their control bits).
 template <class P, int R, int B, int CLS>
-__device__ __forceinline__ void reg_pairs(typename P::Amp (&v)[1 << R], int sub, const typename P::K4 &k,
-                                          uint32_t creg) {
+__device__ __forceinline__ void reg_pairs(typename P::Amp (&v)[1 << R], const TileGate &g, uint32_t jm) {
+    if constexpr (B < R) {
+        const typename P::K4 k = P::load(g);
+        const int sub = g.sub;
 #pragma unroll
-    for (int jj = 0; jj < (1 << (R - 1)); jj++) {
-        const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
-        const int j1 = j0 | (1 << B);
-        if (KBWG_CTRL_OK(j0)) {
-            if (CLS == TG_X) {
-                const typename P::Amp t = v[j0];
-                v[j0] = v[j1];
-                v[j1] = t;
-            }
-            if (CLS == TG_Y) P::y_pair(v[j0], v[j1]);
-            if constexpr (P::kRot) {
-                if (CLS == TG_RY) P::rot_pair(sub, k, v[j0], v[j1]);
-            } else {
-                if (CLS == TG_H) P::h_pair(sub, k, v[j0], v[j1]);
-                if (CLS == TG_RX) P::rx_pair(k, v[j0], v[j1]);
-                if (CLS == TG_RY) P::ry_pair(k, v[j0], v[j1]);
+        for (int jj = 0; jj < (1 << (R - 1)); jj++) {
+            const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
+            const int j1 = j0 | (1 << B);
+            if (KBWG_JM(j0)) {
+                if constexpr (CLS == TG_X) {
+                    const typename P::Amp t = v[j0];
+                    v[j0] = v[j1];
+                    v[j1] = t;
+                }
+                if constexpr (CLS == TG_Y) P::y_pair(v[j0], v[j1]);
+                if constexpr (CLS == TG_H) P::h_pair(sub, k, v[j0], v[j1]);
+                if constexpr (CLS == TG_RX) P::rx_pair(k, v[j0], v[j1]);
+                if constexpr (CLS == TG_RY) P::ry_pair(k, v[j0], v[j1]);
             }
         }
     }
 }
 
+// Gate on lane bit tb: the partner is in lane ^ (1 << tb).  Every lane takes
+// part in the shuffle; register j is updated when fok and (j & creg) == creg.
+// (The predicate is formed at its use: the register mask jm, held as
+// predicates across the shuffles, exhausts the predicate registers.)
 template <class P, int R, int CLS>
-__device__ __forceinline__ void reg_gate(typename P::Amp (&v)[1 << R], int sub, const typename P::K4 &k, int b,
-                                         uint32_t creg) {
-    switch (b) {
-    case 0: reg_pairs<P, R, 0, CLS>(v, sub, k, creg); break;
-    case 1: reg_pairs<P, R, 1, CLS>(v, sub, k, creg); break;
-    case 2: reg_pairs<P, R, 2, CLS>(v, sub, k, creg); break;
-    case 3:
-        if constexpr (R > 3) reg_pairs<P, R, (R > 3 ? 3 : 0), CLS>(v, sub, k, creg);
-        break;
-    default:
-        if constexpr (R > 4) reg_pairs<P, R, (R > 4 ? 4 : 0), CLS>(v, sub, k, creg);
-        break;
+__device__ __forceinline__ void lane_gate(typename P::Amp (&v)[1 << R], const TileGate &g, bool fok, uint32_t F) {
+    constexpr int NR = 1 << R;
+    const uint32_t creg = g.creg;
+#define KBWG_LANE_ON(j) (fok && ((uint32_t)(j) & creg) == creg)
+    const uint32_t tb = g.tb;
+    const bool one = ((F >> tb) & 1u) != 0;
+    const int m = 1 << tb;
+    const typename P::K4 k = P::load(g);
+    if constexpr (CLS == TG_X) {
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp o = P::shfl(v[j], m);
+            if (KBWG_LANE_ON(j)) v[j] = o;
+        }
+    } else if constexpr (CLS == TG_Y) {
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp o = P::shfl(v[j], m);
+            if (KBWG_LANE_ON(j)) v[j] = P::y_half(o, one);
+        }
+    } else if constexpr (CLS == TG_H) {
+        const auto sg = P::sign(one);
+        const int sub = g.sub;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp o = P::shfl(v[j], m);
+            if (KBWG_LANE_ON(j)) v[j] = P::h_half(sub, k, v[j], o, sg);
+        }
+    } else if constexpr (CLS == TG_RX) {
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp o = P::shfl(v[j], m);
+            if (KBWG_LANE_ON(j)) v[j] = P::rx_half(k, v[j], o);
+        }
+    } else {
+        const auto ss = P::signed_s(k, one);
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const typename P::Amp o = P::shfl(v[j], m);
+            if (KBWG_LANE_ON(j)) v[j] = P::ry_half(k, v[j], o, ss);
+        }
     }
+#undef KBWG_LANE_ON
 }
 
 // Diagonal gate on register bit B: the side of every register is known at
 // compile time.
-template <class P, int R, int B>
-__device__ __forceinline__ void diag_reg(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
-                                         uint32_t creg) {
-    constexpr int NR = 1 << R;
-    if constexpr (P::kRot) {
-        if (cls == TG_Z) {
+template <class P, int R, int B, int CLS>
+__device__ __forceinline__ void diag_reg(typename P::Amp (&v)[1 << R], const TileGate &g, uint32_t jm) {
+    if constexpr (B < R) {
+        constexpr int NR = 1 << R;
+        const typename P::K4 k = P::load(g);
 #pragma unroll
-            for (int j = 0; j < NR; j++)
-                if ((j >> B) & 1)
-                    if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
-        } else if (cls == TG_PI) {
-            const int q = (int)reinterpret_cast<const float &>(k.c0);
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if ((j >> B) & 1)
-                    if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
-        } else {
-            if (cls == TG_RZ) {
-#pragma unroll
-                for (int j = 0; j < NR; j++)
-                    if (!((j >> B) & 1))
-                        if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
+        for (int j = 0; j < NR; j++) {
+            if (!KBWG_JM(j)) continue;
+            const bool hi = ((j >> B) & 1) != 0;
+            if constexpr (CLS == TG_Z) {
+                if (hi) v[j] = P::neg(v[j]);
+            } else if constexpr (CLS == TG_P) {
+                if (hi) v[j] = P::cmul(v[j], k.c0, k.c1);
+            } else if constexpr (CLS == TG_RZ) {
+                v[j] = hi ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1);
+            } else {  // TG_PI
+                if (hi) v[j] = P::pi_mul(v[j], (int)reinterpret_cast<const float &>(k.c0));
             }
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if ((j >> B) & 1)
-                    if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c2, k.c3);
         }
-        return;
-    }
-    switch (cls) {
-    case TG_Z:
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if ((j >> B) & 1)
-                if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
-        break;
-    case TG_P:
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if ((j >> B) & 1)
-                if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
-        break;
-    case TG_RZ:
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = ((j >> B) & 1) ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1);
-        break;
-    default: {  // TG_PI
-        const int q = (int)reinterpret_cast<const float &>(k.c0);
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if ((j >> B) & 1)
-                if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
-        break;
-    }
     }
 }
 
 // Diagonal gate whose target bit is the same for all of this thread's
 // registers (a lane/warp bit, or a qubit outside the tile): `one` is uniform.
-template <class P, int R>
-__device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
-                                           uint32_t creg, bool one) {
+template <class P, int R, int CLS>
+__device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], const TileGate &g, uint32_t jm, bool one) {
     constexpr int NR = 1 << R;
-    if constexpr (P::kRot) {
-        if (cls == TG_SCALE) one = true;
-        if (!one && cls != TG_RZ) return;
-        if (cls == TG_Z) {
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
-        } else if (cls == TG_PI) {
-            const int q = (int)reinterpret_cast<const float &>(k.c0);
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
-        } else {
-            const auto c = one ? k.c2 : k.c0;
-            const auto s = one ? k.c3 : k.c1;
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], c, s);
-        }
-        return;
-    }
-    if (cls == TG_SCALE) {
+    if constexpr (CLS != TG_SCALE && CLS != TG_RZ)
+        if (!one) return;
+    const typename P::K4 k = P::load(g);
+    if constexpr (CLS == TG_Z) {
 #pragma unroll
         for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
-        return;
-    }
-    if (cls == TG_RZ) {
-        const auto c = one ? k.c2 : k.c0;
-        const auto s = one ? k.c3 : k.c1;
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], c, s);
-        return;
-    }
-    if (!one) return;
-    if (cls == TG_Z) {
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = P::neg(v[j]);
-    } else if (cls == TG_P) {
-#pragma unroll
-        for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = P::cmul(v[j], k.c0, k.c1);
-    } else {  // TG_PI
+            if (KBWG_JM(j)) v[j] = P::neg(v[j]);
+    } else if constexpr (CLS == TG_PI) {
         const int q = (int)reinterpret_cast<const float &>(k.c0);
 #pragma unroll
         for (int j = 0; j < NR; j++)
-            if (KBWG_CTRL_OK(j)) v[j] = P::pi_mul(v[j], q);
+            if (KBWG_JM(j)) v[j] = P::pi_mul(v[j], q);
+    } else {
+        // P: |1> * (c0, c1); SCALE: all * (c0, c1); RZ: (c0, c1) or (c2, c3)
+        const auto c = (CLS == TG_RZ && one) ? k.c2 : k.c0;
+        const auto s = (CLS == TG_RZ && one) ? k.c3 : k.c1;
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+            if (KBWG_JM(j)) v[j] = P::cmul(v[j], c, s);
     }
-}
-
-template <class P, int R, int B>
-__device__ __forceinline__ void reg_dispatch(typename P::Amp (&v)[1 << R], int cls, int sub,
-                                             const typename P::K4 &k, uint32_t creg) {
-    if constexpr (B < R && P::kRot) {
-        switch (cls) {
-        case TG_X: reg_pairs<P, R, B, TG_X>(v, sub, k, creg); break;
-        case TG_Y: reg_pairs<P, R, B, TG_Y>(v, sub, k, creg); break;
-        default: reg_pairs<P, R, B, TG_RY>(v, sub, k, creg); break;
-        }
-    } else if constexpr (B < R) {
-        switch (cls) {
-        case TG_X: reg_pairs<P, R, B, TG_X>(v, sub, k, creg); break;
-        case TG_Y: reg_pairs<P, R, B, TG_Y>(v, sub, k, creg); break;
-        case TG_H: reg_pairs<P, R, B, TG_H>(v, sub, k, creg); break;
-        case TG_RX: reg_pairs<P, R, B, TG_RX>(v, sub, k, creg); break;
-        default: reg_pairs<P, R, B, TG_RY>(v, sub, k, creg); break;
-        }
-    }
-}
-
-template <class P, int R, int B>
-__device__ __forceinline__ void dreg_dispatch(typename P::Amp (&v)[1 << R], int cls, const typename P::K4 &k,
-                                              uint32_t creg) {
-    if constexpr (B < R) diag_reg<P, R, B>(v, cls, k, creg);
 }
 
 // Apply one gate to the thread's registers.  F = the thread's fixed local
-// bits (lane and warp).  The gate's op/rb/fneed/creg were computed by the
-// planner for the layout this stage runs in.
+// bits (lane and warp) in this stage's layout; base = the tile's global
+// index of local 0.  A few header loads and one jump table per gate.
 template <class P, int K, int R>
 __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int /*R0*/, uint32_t F,
                                           uint64_t base) {
     static_assert(R >= 3 && R <= 4, "dispatch covers register bits 0..3");
-    constexpr int NR = 1 << R;
-    if ((base & g.co) != g.co) return;  // a control outside the tile is 0 for the whole tile
-    const bool fok = (F & g.fneed) == g.fneed;
     const uint32_t op = g.op;
-    const uint32_t creg = g.creg;
-    if (op < OP_REG) {
-        // lane-bit target: every lane takes part in the shuffle (a control is
-        // never the target, so both halves of a pair share control values)
-        const typename P::K4 k = P::load(g);
-        const uint32_t tb = g.tb;
-        const bool one = ((F >> tb) & 1u) != 0;
-        const int m = 1 << tb;
-        if constexpr (P::kRot) {
-            if (op == OP_LANE + TG_X) {
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    const typename P::Amp o = P::shfl(v[j], m);
-                    if (fok && KBWG_CTRL_OK(j)) v[j] = o;
-                }
-            } else if (op == OP_LANE + TG_Y) {
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    const typename P::Amp o = P::shfl(v[j], m);
-                    if (fok && KBWG_CTRL_OK(j)) v[j] = P::y_half(o, one);
-                }
-            } else {
-                const auto A = one ? k.c3 : k.c0;
-                const auto Bc = one ? k.c2 : k.c1;
-                const bool mm = g.sub != 0;
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    const typename P::Amp o = P::shfl(v[j], m);
-                    if (fok && KBWG_CTRL_OK(j)) v[j] = P::rot_half(A, Bc, mm, v[j], o);
-                }
-            }
-            return;
-        } else {
-        switch (op) {
-        case OP_LANE + TG_X:
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && KBWG_CTRL_OK(j)) v[j] = o;
-            }
-            break;
-        case OP_LANE + TG_Y:
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && KBWG_CTRL_OK(j)) v[j] = P::y_half(o, one);
-            }
-            break;
-        case OP_LANE + TG_H: {
-            const auto sg = P::sign(one);
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && KBWG_CTRL_OK(j)) v[j] = P::h_half(g.sub, k, v[j], o, sg);
-            }
-            break;
-        }
-        case OP_LANE + TG_RX:
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && KBWG_CTRL_OK(j)) v[j] = P::rx_half(k, v[j], o);
-            }
-            break;
-        default: {
-            const auto ss = P::signed_s(k, one);
-#pragma unroll
-            for (int j = 0; j < NR; j++) {
-                const typename P::Amp o = P::shfl(v[j], m);
-                if (fok && KBWG_CTRL_OK(j)) v[j] = P::ry_half(k, v[j], o, ss);
-            }
-            break;
-        }
-        }
+    const uint32_t fneed = g.fneed;
+    const uint32_t jm = g.jm;
+    if ((base & g.co) != g.co) return;  // a control outside the tile is 0 for the whole tile
+    const bool fok = (F & fneed) == fneed;
+    if (op < OP_REG) {  // lane targets: every lane shuffles, outside the jump table
+        if (op == OP_LANE + TG_X) lane_gate<P, R, TG_X>(v, g, fok, F);
+        else if (op == OP_LANE + TG_Y) lane_gate<P, R, TG_Y>(v, g, fok, F);
+        else if (op == OP_LANE + TG_H) lane_gate<P, R, TG_H>(v, g, fok, F);
+        else if (op == OP_LANE + TG_RX) lane_gate<P, R, TG_RX>(v, g, fok, F);
+        else lane_gate<P, R, TG_RY>(v, g, fok, F);
         return;
-        }
     }
     if (!fok) return;
-    const typename P::K4 k = P::load(g);
-    if (op < OP_DREG) {
-        const int c = (int)(op - OP_REG) >> 2;
-        switch ((op - OP_REG) & 3u) {
-        case 0: reg_dispatch<P, R, 0>(v, c, g.sub, k, creg); break;
-        case 1: reg_dispatch<P, R, 1>(v, c, g.sub, k, creg); break;
-        case 2: reg_dispatch<P, R, 2>(v, c, g.sub, k, creg); break;
-        default: reg_dispatch<P, R, 3>(v, c, g.sub, k, creg); break;
-        }
-        return;
+    switch (op) {
+#define KBWG_REG(C)                                                    \
+    case OP_REG + C * 4 + 0: reg_pairs<P, R, 0, C>(v, g, jm); break; \
+    case OP_REG + C * 4 + 1: reg_pairs<P, R, 1, C>(v, g, jm); break; \
+    case OP_REG + C * 4 + 2: reg_pairs<P, R, 2, C>(v, g, jm); break; \
+    case OP_REG + C * 4 + 3: reg_pairs<P, R, 3, C>(v, g, jm); break;
+#define KBWG_DREG(C)                                                               \
+    case OP_DREG + (C - TG_Z) * 4 + 0: diag_reg<P, R, 0, C>(v, g, jm); break; \
+    case OP_DREG + (C - TG_Z) * 4 + 1: diag_reg<P, R, 1, C>(v, g, jm); break; \
+    case OP_DREG + (C - TG_Z) * 4 + 2: diag_reg<P, R, 2, C>(v, g, jm); break; \
+    case OP_DREG + (C - TG_Z) * 4 + 3: diag_reg<P, R, 3, C>(v, g, jm); break;
+#define KBWG_DFIX(C)                                                                                          \
+    case OP_DFIX + (C - TG_Z): {                                                                           \
+        const uint32_t tb = g.tb, tout = g.tout;                                    \
+        const bool one = (C == TG_SCALE) || (tb == TG_OUTER ? ((base >> tout) & 1ull) != 0 : ((F >> tb) & 1u) != 0); \
+        diag_fixed<P, R, C>(v, g, jm, one);                                                                 \
+        break;                                                                                              \
     }
-    if (op < OP_DFIX) {
-        const int c = TG_Z + ((int)(op - OP_DREG) >> 2);
-        switch ((op - OP_DREG) & 3u) {
-        case 0: dreg_dispatch<P, R, 0>(v, c, k, creg); break;
-        case 1: dreg_dispatch<P, R, 1>(v, c, k, creg); break;
-        case 2: dreg_dispatch<P, R, 2>(v, c, k, creg); break;
-        default: dreg_dispatch<P, R, 3>(v, c, k, creg); break;
-        }
-        return;
+        KBWG_REG(TG_X) KBWG_REG(TG_Y) KBWG_REG(TG_H) KBWG_REG(TG_RX) KBWG_REG(TG_RY)
+        KBWG_DREG(TG_Z) KBWG_DREG(TG_P) KBWG_DREG(TG_RZ) KBWG_DREG(TG_PI)
+        KBWG_DFIX(TG_Z) KBWG_DFIX(TG_P) KBWG_DFIX(TG_RZ) KBWG_DFIX(TG_PI) KBWG_DFIX(TG_SCALE)
+#undef KBWG_REG
+#undef KBWG_DREG
+#undef KBWG_DFIX
+    default: break;
     }
-    const int c = TG_Z + (int)(op - OP_DFIX);
-    const bool one = (c == TG_SCALE) ? true
-                     : (g.tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0)
-                                          : (((F >> g.tb) & 1u) != 0);
-    diag_fixed<P, R>(v, c, k, creg, one);
 }
 
-#undef KBWG_CTRL_OK
+#undef KBWG_JM
 
 }  // namespace kbwg
