@@ -216,6 +216,25 @@ def time_steps(sim, circ, steps, warmup, torch):
     return e0.elapsed_time(e1) / steps, nl, kms, kbytes
 
 
+def single_gate_sweep(sim, torch, peak, C, reps=5):
+    """CUDA-event time of sweeps that each apply one RZ (the lightest full
+    read + write of the state through the tile kernel)."""
+    g = [(C.RZ, 3, (), 0.3)]
+    sim.apply(g)
+    sim.flush()
+    sim.profile(True)
+    torch.cuda.synchronize()
+    for _ in range(reps):
+        sim.apply(g)
+        sim.flush()
+    torch.cuda.synchronize()
+    nl, kms, kbytes = sim.profile_read()
+    sim.profile(False)
+    ach = kbytes / (kms * 1e-3) / 1e9
+    return {"achieved": round(ach, 1), "frac": round(ach / peak, 4), "unit": "GB/s",
+            "avg_launch_ms": round(kms / max(nl, 1), 4), "launches": nl}
+
+
 def run_adjoint_bench(args, torch, DenseGB300, C):
     """Gradient half of the metric: 24 qubits, 10 layers of RY, RZ on every
     qubit + CZ ring (480 parameters), ring TFIM.  grads/s of the adjoint
@@ -256,6 +275,38 @@ def run_adjoint_bench(args, torch, DenseGB300, C):
         out[label] = item
         sim.close()
     return out
+
+
+def run_adjoint_large(args, torch, DenseGB300, C):
+    """Large adjoint gradient: 32 qubits in complex64 (32 GiB per state; the
+    state, lambda and one checkpoint), 6 layers of RY, RZ + CZ ring (384
+    parameters), ring TFIM.  Its error is stated on a 28-qubit replica of the
+    same structure: complex64 against the complex128 (float-float) adjoint."""
+    n, L = args.adj_large_qubits, 6
+    params = C.hea_params(n, L, 0)
+    circ, pidx, ham = C.hea(n, L, params), C.hea_param_index(n, L), C.tfim_ring(n)
+    sim = DenseGB300(n, "c64")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e, g = sim.adjoint_gradient(circ, pidx, len(params), ham, max_checkpoints=1)
+    torch.cuda.synchronize()
+    ta = time.perf_counter() - t0
+    sim.close()
+    del sim
+    nr = min(28, n)
+    pr = C.hea_params(nr, L, 0)
+    cr, ir, hr = C.hea(nr, L, pr), C.hea_param_index(nr, L), C.tfim_ring(nr)
+    res = {}
+    for label, prec, fast in (("c64", "c64", False), ("c128_ff", "c128", True)):
+        r = DenseGB300(nr, prec, fast_c128=fast)
+        res[label] = r.adjoint_gradient(cr, ir, len(pr), hr)
+        r.close()
+    return {"config": "hea-%dq-%dlayers-%dparams-tfim-ring c64" % (n, L, len(params)), "energy": e,
+            "adjoint_s": round(ta, 3), "adjoint_grads_per_s": round(len(params) / ta, 1),
+            "state_gib": (8 << n) >> 30, "buffers": "state + lambda + 1 checkpoint",
+            "replica": {"qubits": nr, "max_grad_err_c64_vs_c128": float(np.max(np.abs(res["c64"][1] -
+                                                                                        res["c128_ff"][1]))),
+                        "abs_dE_c64_vs_c128": abs(res["c64"][0] - res["c128_ff"][0])}}
 
 
 def run_batch_bench(args, torch, C):
@@ -341,11 +392,15 @@ def run_ours(args, world, rank, local):
     value = world * step_bytes / (ms_step * 1e-3) / 1e9
 
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else None
-    kname = "k_sweep<%s>" % ({"c64": "Exact<float>", "c128": "FFPol" if fast else "Exact<double>"}[prec])
+    kname = "k_sweep<%s>" % ({"c64": "Fast<float>", "c128": "FF2" if fast else "Fast<double>"}[prec])
     roofline = {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None, "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                 "traffic": args.traffic, "kernel": kname, "launches": nl,
                 "avg_launch_ms": round(kms / max(nl, 1), 4), "peak_source": peak_kind + " hbm_gbs (burst copy)"}
+
+    # one gate per sweep: the bandwidth of plain gate application, the bar a
+    # one-gate-per-pass engine is held to (fusion then packs ~25 gates a sweep)
+    single = single_gate_sweep(sim, torch, peak, C)
 
     # ---- e2e through the C ABI, host buffers ----
     zs = [(1.0, [(C.PAULI_Z, q)]) for q in range(n)]
@@ -403,17 +458,22 @@ def run_ours(args, world, rank, local):
         s64 = DenseGB300(n, "c64")
         ms64, nl64, kms64, kb64 = time_steps(s64, circ, args.steps, 2, torch)
         ach64 = kb64 / (kms64 * 1e-3) / 1e9
+        sweeps64 = s64.last_flush_stats()[1]
+        single64 = single_gate_sweep(s64, torch, peak, C)
         secondary["c64"] = {"value": round(G * 2 * 8 * (1 << n) / (ms64 * 1e-3) / 1e9, 1), "unit": "GB/s",
-                            "ms_per_step": round(ms64, 3), "sweeps_per_step": s64.last_flush_stats()[1],
+                            "ms_per_step": round(ms64, 3), "sweeps_per_step": sweeps64,
                             "dtype": "f32",
                             "roofline": {"achieved": round(ach64, 1), "frac": round(ach64 / peak, 4),
-                                         "avg_launch_ms": round(kms64 / max(nl64, 1), 4)}}
+                                         "avg_launch_ms": round(kms64 / max(nl64, 1), 4)},
+                            "single_gate_sweep": single64}
         s64.close()
     else:
         sim.close()
 
     if args.adjoint:
         secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C)
+    if args.adjoint_large:
+        secondary["adjoint_large"] = run_adjoint_large(args, torch, DenseGB300, C)
     if args.batch:
         secondary["batch"] = run_batch_bench(args, torch, C)
 
@@ -430,7 +490,7 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32x2 (float-float, binary64 in HBM)" if fast else ("f64" if prec == "c128" else "f32"),
+            "dtype": "f32x2 (float-float; binary64 at the API)" if fast else ("f64" if prec == "c128" else "f32"),
             "data": "synthetic: seeded random brickwork circuit (numpy default_rng(0))",
             "config": {"workload": "brickwork-%dq-%dlayers-%s" % (n, args.layers, prec), "qubits": n,
                        "layers": args.layers, "gates": G, "precision": prec,
@@ -439,7 +499,7 @@ def run_ours(args, world, rank, local):
                        "parallelism": "replicas" if world > 1 else "single"},
             "sweep_gbs": round(world * passes * 2 * B * (1 << n) / (ms_step * 1e-3) / 1e9, 1),
             "gpu_launches": launches,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "roofline": roofline, "single_gate_sweep": single, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         line.update(secondary)
         print(json.dumps(line), flush=True)
@@ -463,6 +523,8 @@ def main():
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--no-adjoint-large", dest="adjoint_large", action="store_false")
+    ap.add_argument("--adj-large-qubits", type=int, default=32)
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--adj-qubits", type=int, default=24)

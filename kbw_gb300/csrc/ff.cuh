@@ -74,7 +74,8 @@ FFI float u2f(uint32_t r) { return (float)r; }
 FFI int f2i(float q) { return (int)lrintf(q); }
 #endif
 
-FFI float neg(float a) { return bitsf(fbits(a) ^ 0x80000000u); }
+// Exact; as an operand it folds into the consuming instruction's negate modifier.
+FFI float neg(float a) { return -a; }
 FFI f2 neg(f2 a) { return f2{neg(a.h), neg(a.l)}; }
 
 FFI f2 two_sum(float a, float b) {

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) k_init_zero_state(cx<T> *__restrict__ st,
     }
 }
 
-// |0...0> as float-float pairs: amplitude 0 is (hi 1, lo 0, 0, 0); zero
+// |0...0> in float-float form: amplitude 0 is (re.hi 1, 0, 0, 0); zero
 // amplitudes have the same all-zero bytes in both formats.
 __global__ void __launch_bounds__(256) k_init_zero_state_ff(float4 *__restrict__ st, uint64_t ns) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -53,16 +53,17 @@ __global__ void __launch_bounds__(256) k_init_zero_state_ff(float4 *__restrict__
 }
 
 // binary64 <-> float-float, in place (each thread rewrites its own 16 bytes).
+// Float-float layout per amplitude: re.hi, im.hi, re.lo, im.lo.
 __global__ void __launch_bounds__(256) k_ff_convert(cx<double> *__restrict__ st, uint64_t ns, int to_ff) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
         if (to_ff) {
             const cx<double> a = st[s];
             const ff::f2 re = ff::from_double(a.re), im = ff::from_double(a.im);
-            reinterpret_cast<float4 *>(st)[s] = make_float4(re.h, re.l, im.h, im.l);
+            reinterpret_cast<float4 *>(st)[s] = make_float4(re.h, im.h, re.l, im.l);
         } else {
             const float4 f = reinterpret_cast<const float4 *>(st)[s];
-            st[s] = cx<double>{ff::to_double(ff::f2{f.x, f.y}), ff::to_double(ff::f2{f.z, f.w})};
+            st[s] = cx<double>{ff::to_double(ff::f2{f.x, f.z}), ff::to_double(ff::f2{f.y, f.w})};
         }
     }
 }

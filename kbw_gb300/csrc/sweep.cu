@@ -323,7 +323,7 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
             s.ff_resident = true;
         }
         std::vector<GateDesc> g = ff_rewrite(gates, count);
-        return run_fused_p<FFRes, TileCfg<double>::K, TileCfg<double>::R>(s, g.data(), g.size());
+        return run_fused_p<FF2, TileCfg<double>::K, TileCfg<double>::R>(s, g.data(), g.size());
     }
     return s.prec ? run_fused_t<double>(s, gates, count) : run_fused_t<float>(s, gates, count);
 }

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include "ff.cuh"
+#include "ff2.cuh"
 #include "sweep.h"
 
 namespace kbwg {
@@ -272,13 +273,83 @@ struct FFPol {
     }
 };
 
-// Float-float policy with the state resident in float-float form in HBM
-// (per amplitude: hi, lo of the real part, then hi, lo of the imaginary
-// part; 16 bytes like binary64): sweeps load and store it unconverted.
-struct FFRes : FFPol {
-    using Mem = FFPol::Amp;
+// Packed float-float policy, state resident in float-float form in HBM:
+// per amplitude h = (re.hi, im.hi), l = (re.lo, im.lo) (16 bytes, like
+// binary64), loaded and stored unconverted.  The arithmetic is FFPol's, lane
+// by lane, on f32x2 instructions: each FADD2/FMUL2/FFMA2 advances the real
+// and the imaginary part together, halving the instruction count of the
+// gate bodies (and their code size) at the same FP32 pipe time.
+struct FF2 {
+    using Amp = ff2::v2;
+    using Mem = ff2::v2;
+    using Scalar = ff::f2;
+    using K4 = FFPol::K4;
     static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
+    static void pack_host(TileGate &g) { FFPol::pack_host(g); }
+    static __device__ __forceinline__ K4 load(const TileGate &g) { return FFPol::load(g); }
+    static __device__ __forceinline__ Amp shfl(Amp v, int m) {
+        Amp r;
+        r.h.x = __shfl_xor_sync(0xffffffffu, v.h.x, m);
+        r.h.y = __shfl_xor_sync(0xffffffffu, v.h.y, m);
+        r.l.x = __shfl_xor_sync(0xffffffffu, v.l.x, m);
+        r.l.y = __shfl_xor_sync(0xffffffffu, v.l.y, m);
+        return r;
+    }
+    static __device__ __forceinline__ Amp neg(Amp a) { return ff2::neg(a); }
+    static __device__ __forceinline__ void y_pair(Amp &a0, Amp &a1) {
+        const Amp n0 = ff2::mul_minus_i(a1), n1 = ff2::mul_i(a0);
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp y_half(Amp o, bool one) { return one ? ff2::mul_i(o) : ff2::mul_minus_i(o); }
+    static __device__ __forceinline__ void h_pair(int sub, const K4 &k, Amp &a0, Amp &a1) {
+        Amp n0 = ff2::add(a0, a1), n1 = ff2::sub(a0, a1);
+        if (sub == 0) {
+            const ff2::k2 c = ff2::konst(k.c0);
+            n0 = ff2::mul(n0, c);
+            n1 = ff2::mul(n1, c);
+        }
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp h_half(int sub, const K4 &k, Amp self, Amp o, ff::f2 sgn) {
+        const bool one = sgn.h < 0.f;
+        Amp r = one ? ff2::sub(o, self) : ff2::add(self, o);
+        if (sub == 0) r = ff2::mul(r, ff2::konst(k.c0));
+        return r;
+    }
+    // RX: out0 = c a0 + s (a1.im, -a1.re), out1 = c a1 + s (a0.im, -a0.re)
+    static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const ff2::k2 c = ff2::konst(k.c0), s = ff2::konst(k.c1, ff::neg(k.c1));
+        const Amp n0 = ff2::dot2(c, a0, s, ff2::swap(a1)), n1 = ff2::dot2(c, a1, s, ff2::swap(a0));
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp rx_half(const K4 &k, Amp self, Amp o) {
+        return ff2::dot2(ff2::konst(k.c0), self, ff2::konst(k.c1, ff::neg(k.c1)), ff2::swap(o));
+    }
+    // RY: out0 = c a0 - s a1, out1 = c a1 + s a0
+    static __device__ __forceinline__ void ry_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const ff2::k2 c = ff2::konst(k.c0), s = ff2::konst(k.c1), ns = ff2::konst(ff::neg(k.c1));
+        const Amp n0 = ff2::dot2(c, a0, ns, a1), n1 = ff2::dot2(c, a1, s, a0);
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ ff::f2 signed_s(const K4 &k, bool one) { return one ? k.c1 : ff::neg(k.c1); }
+    static __device__ __forceinline__ ff::f2 sign(bool one) { return one ? ff::f2{-1.f, 0.f} : ff::f2{1.f, 0.f}; }
+    static __device__ __forceinline__ Amp ry_half(const K4 &k, Amp self, Amp o, ff::f2 ss) {
+        return ff2::dot2(ff2::konst(k.c0), self, ff2::konst(ss), o);
+    }
+    // a * (c + i s): (c re - s im, c im + s re) = c (re, im) + (-s, s) (im, re)
+    static __device__ __forceinline__ Amp cmul(Amp a, ff::f2 c, ff::f2 s) {
+        return ff2::dot2(ff2::konst(c), a, ff2::konst(ff::neg(s), s), ff2::swap(a));
+    }
+    static __device__ __forceinline__ Amp pi_mul(Amp a, int q) {
+        if (q == 1) return ff2::mul_i(a);
+        if (q == 2) return ff2::neg(a);
+        return ff2::mul_minus_i(a);
+    }
 };
 
 // ---- per-gate register code -------------------------------------------------------
