@@ -22,8 +22,19 @@ struct k2 {
 
 __device__ __forceinline__ float2 pk(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-// a - b, exact as one FFMA2: (-1) * b + a rounded once
-__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// a - b in one packed instruction (the runtime headers offer no packed
+// subtract; PTX sub.rn.f32x2 folds the negation into the FADD2)
+union f2bits {
+    float2 f;
+    unsigned long long u;
+};
+__device__ __forceinline__ float2 sub(float2 a, float2 b) {
+    f2bits x, y, d;
+    x.f = a;
+    y.f = b;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.u) : "l"(x.u), "l"(y.u));
+    return d.f;
+}
 __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
@@ -91,7 +102,9 @@ __device__ __forceinline__ v2 dot2(const k2 &c, v2 x, const k2 &s, v2 y) {
 
 // lane swap (re <-> im)
 __device__ __forceinline__ v2 swap(v2 a) { return v2{pk(a.h.y, a.h.x), pk(a.l.y, a.l.x)}; }
-__device__ __forceinline__ v2 neg(v2 a) { return v2{pk(-a.h.x, -a.h.y), pk(-a.l.x, -a.l.y)}; }
+// exact negation on the FMA pipe (keeps the sign of zero, like -x)
+__device__ __forceinline__ float2 neg(float2 a) { return mul(a, make_float2(-1.f, -1.f)); }
+__device__ __forceinline__ v2 neg(v2 a) { return v2{neg(a.h), neg(a.l)}; }
 // (re, im) -> (im, -re) = -i * a   and   (-im, re) = i * a
 __device__ __forceinline__ v2 mul_minus_i(v2 a) { return v2{pk(a.h.y, -a.h.x), pk(a.l.y, -a.l.x)}; }
 __device__ __forceinline__ v2 mul_i(v2 a) { return v2{pk(-a.h.y, a.h.x), pk(-a.l.y, a.l.x)}; }

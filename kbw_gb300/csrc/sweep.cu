@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include <math.h>
 
@@ -228,7 +229,8 @@ static cudaError_t run_fused_t(Sim &s, const GateDesc *gates, size_t count) {
         return cudaSuccess;
     }
     if (s.flags & KBWG_FLAG_EXACT_ORDER) return run_fused_p<Exact<T>, K, R>(s, gates, count);
-    return run_fused_p<Fast<T>, K, R>(s, gates, count);
+    if constexpr (std::is_same<T, float>::value) return run_fused_p<FastP, K, R>(s, gates, count);
+    else return run_fused_p<Fast<T>, K, R>(s, gates, count);
 }
 
 // Complex128 float-float path: rewrite the queue so that uncontrolled H

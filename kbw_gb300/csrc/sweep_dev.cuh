@@ -173,6 +173,71 @@ struct Fast : Exact<T> {
     }
 };
 
+// Fast for complex64 on packed f32x2 instructions: an amplitude is one
+// float2 (re, im) and every step advances both parts with one
+// FADD2/FMUL2/FFMA2 (the real-coefficient rotations lane by lane as Fast;
+// the complex product pairs (re, im) * c with (im, re) * (-s, s)).
+struct FastP {
+    using Amp = float2;
+    using Mem = cx<float>;
+    using Scalar = float;
+    using K4 = Exact<float>::K4;
+    static __device__ __forceinline__ Amp from_mem(Mem a) { return make_float2(a.re, a.im); }
+    static __device__ __forceinline__ Mem to_mem(Amp a) { return Mem{a.x, a.y}; }
+    static void pack_host(TileGate &g) { Exact<float>::pack_host(g); }
+    static __device__ __forceinline__ K4 load(const TileGate &g) { return Exact<float>::load(g); }
+    static __device__ __forceinline__ Amp shfl(Amp v, int m) {
+        return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+    }
+    static __device__ __forceinline__ float2 bc(float x) { return make_float2(x, x); }
+    static __device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }
+    static __device__ __forceinline__ Amp neg(Amp a) { return ff2::neg(a); }
+    static __device__ __forceinline__ void y_pair(Amp &a0, Amp &a1) {
+        const Amp n0 = make_float2(a1.y, -a1.x), n1 = make_float2(-a0.y, a0.x);
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp y_half(Amp o, bool one) {
+        return one ? make_float2(-o.y, o.x) : make_float2(o.y, -o.x);
+    }
+    static __device__ __forceinline__ void h_pair(int, const K4 &k, Amp &a0, Amp &a1) {
+        const float2 c = bc(k.c0);
+        const Amp n0 = __fmul2_rn(__fadd2_rn(a0, a1), c);
+        const Amp n1 = __fmul2_rn(ff2::sub(a0, a1), c);
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp h_half(int, const K4 &k, Amp self, Amp o, float sgn) {
+        return __fmul2_rn(__ffma2_rn(bc(sgn), self, o), bc(k.c0));
+    }
+    static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const float2 c = bc(k.c0), s = make_float2(k.c1, -k.c1);
+        const Amp n0 = __ffma2_rn(c, a0, __fmul2_rn(s, swp(a1)));
+        const Amp n1 = __ffma2_rn(c, a1, __fmul2_rn(s, swp(a0)));
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ Amp rx_half(const K4 &k, Amp self, Amp o) {
+        return __ffma2_rn(bc(k.c0), self, __fmul2_rn(make_float2(k.c1, -k.c1), swp(o)));
+    }
+    static __device__ __forceinline__ void ry_pair(const K4 &k, Amp &a0, Amp &a1) {
+        const float2 c = bc(k.c0), s = bc(k.c1), ns = bc(-k.c1);
+        const Amp n0 = __ffma2_rn(c, a0, __fmul2_rn(ns, a1));
+        const Amp n1 = __ffma2_rn(c, a1, __fmul2_rn(s, a0));
+        a0 = n0;
+        a1 = n1;
+    }
+    static __device__ __forceinline__ float signed_s(const K4 &k, bool one) { return one ? k.c1 : -k.c1; }
+    static __device__ __forceinline__ float sign(bool one) { return one ? -1.f : 1.f; }
+    static __device__ __forceinline__ Amp ry_half(const K4 &k, Amp self, Amp o, float ss) {
+        return __ffma2_rn(bc(k.c0), self, __fmul2_rn(bc(ss), o));
+    }
+    static __device__ __forceinline__ Amp cmul(Amp a, float c, float s) {
+        return __ffma2_rn(a, bc(c), __fmul2_rn(swp(a), make_float2(-s, s)));
+    }
+    static __device__ __forceinline__ Amp pi_mul(Amp a, int) { return a; }  // float-float path only
+};
+
 // ---- float-float policy (complex128 fast path) ---------------------------------
 // HBM keeps IEEE binary64; amplitudes become hi+lo float pairs on the way in
 // and are rounded back on the way out.  Constants arrive pre-split by
