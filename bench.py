@@ -392,10 +392,16 @@ def run_ours(args, world, rank, local):
     value = world * step_bytes / (ms_step * 1e-3) / 1e9
 
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else None
+    # DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
+    # one k_sweep<FF2> launch on the 25-qubit brickwork (1017.4 MB), scaled to
+    # 2^n amplitudes (traffic grows with the state; one read + write each)
+    traffic = args.traffic
+    if traffic is None and fast:
+        traffic = round(1017.4e6 * (1 << n) / (1 << 25))
     kname = "k_sweep<%s>" % ({"c64": "Fast<float>", "c128": "FF2" if fast else "Fast<double>"}[prec])
     roofline = {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None, "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                "traffic": args.traffic, "kernel": kname, "launches": nl,
+                "traffic": traffic, "kernel": kname, "launches": nl,
                 "avg_launch_ms": round(kms / max(nl, 1), 4), "peak_source": peak_kind + " hbm_gbs (burst copy)"}
 
     # one gate per sweep: the bandwidth of plain gate application, the bar a
@@ -532,7 +538,8 @@ def main():
     ap.add_argument("--adj-reps", type=int, default=3)
     ap.add_argument("--adj-ps-c128", action="store_true", help="also time parameter shift in float-float complex128")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="ncu dram bytes per sweep launch, when known")
+                    help="ncu DRAM bytes (read + write) per sweep launch; default: the 25-qubit capture "
+                         "of k_sweep<FF2> (1017.4 MB) scaled by the amplitude count")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
