@@ -334,3 +334,72 @@ def test_fast_c128_many_hadamards_rescale():
     ref = oracle.OracleDense(n, "c128")
     ref.apply(circ)
     assert rel_err(sim.state(), ref.state()) < 1e-12
+
+
+def test_fast_c128_resident_format_transitions():
+    """The float-float handle keeps its state in float-float form between
+    sweeps and returns to binary64 for every other operation: interleave
+    gates with every kind of read, a swap (format-agnostic), a collapse,
+    set_state and clear, and follow the restated Dense<f64> throughout."""
+    n = 14
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    ref = oracle.OracleDense(n, "c128")
+
+    def step(circ):
+        sim.apply(circ)
+        ref.apply(circ)
+
+    step(C.random_circuit(n, 150, 71, max_controls=2))
+    assert rel_err(sim.state(), ref.state()) < 1e-12        # get_state converts back
+    step(C.brickwork(n, 3, 72))
+    sim.swap_qubits(2, 11)                                  # runs on the float-float form
+    ref.swap_qubits(2, 11)
+    step(C.random_circuit(n, 100, 73))
+    assert abs(sim.measure_p1(5) - ref.measure_p1(5)) < 1e-12
+    p = ref.measure_p1(5)
+    sim.measure_collapse(5, True, 1.0 / math.sqrt(p))
+    ref.measure_collapse(5, True, 1.0 / math.sqrt(p))
+    step(C.random_circuit(n, 100, 74))
+    h = C.tfim_ring(n) + [(0.3, [(C.PAULI_Y, 1), (C.PAULI_Z, 6)])]
+    assert abs(sim.exp_value(h) - ref.exp_value(h)) < 1e-11
+    step(C.random_circuit(n, 60, 75))
+    st, re, im = sim.dump(list(range(n)))
+    rst, rre, rim = ref.dump(list(range(n)))
+    assert np.array_equal(st, rst)
+    assert np.max(np.abs(re - rre)) < 1e-12 and np.max(np.abs(im - rim)) < 1e-12
+    # set_state replaces the resident form; gates after it start from binary64
+    psi = ref.state()
+    sim.set_state(psi)
+    step(C.random_circuit(n, 80, 76))
+    assert rel_err(sim.state(), ref.state()) < 1e-12
+    # clear re-initialises in float-float form
+    sim.clear()
+    ref2 = oracle.OracleDense(n, "c128")
+    circ = C.random_circuit(n, 120, 77)
+    sim.apply(circ)
+    ref2.apply(circ)
+    assert rel_err(sim.state(), ref2.state()) < 1e-12
+    draws = C.uniform_draws(n, 78)
+    assert sim.measure(list(range(n)), draws) == ref2.measure(list(range(n)), draws)
+
+
+def test_fast_c128_distance_and_gradient_after_gates():
+    """state_distance and the adjoint gradient on a handle whose state was
+    left in float-float form by earlier gates."""
+    n = 13
+    a = DenseGB300(n, "c128", fast_c128=True)
+    b = DenseGB300(n, "c128")
+    circ = C.random_circuit(n, 200, 81)
+    a.apply(circ)
+    b.apply(circ)
+    assert a.distance(b) < 1e-12
+    L = 2
+    params = C.hea_params(n, L, 82)
+    pidx = C.hea_param_index(n, L)
+    a.apply(C.random_circuit(n, 50, 83))  # leave a float-float state behind
+    e_a, g_a = a.adjoint_gradient(C.hea(n, L, params), pidx, len(params), C.tfim_ring(n))
+    e_b, g_b = b.adjoint_gradient(C.hea(n, L, params), pidx, len(params), C.tfim_ring(n))
+    assert abs(e_a - e_b) < 1e-11
+    assert np.max(np.abs(g_a - g_b)) < 1e-10
+    # the adjoint leaves |0...0>
+    assert abs(a.state()[0] - 1.0) < 1e-15
