@@ -75,6 +75,30 @@ template <class T>
 cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, const ReduceScratch &rs,
                                cudaStream_t s);
 
+// Pair-form Pauli strings with different flip masks in one pass: a tile of
+// 2^K amplitudes (local bits 0..l-1 = qubits 0..l-1, l..K-1 = qubits hq[])
+// holds both members of every pair of every string whose flip mask lies in
+// the tile.  Per term: <psi|P_k|psi> without coefficient into result[k].
+struct PauliTileTerm {
+    uint32_t xl;    // flip mask on local bits
+    uint32_t zl;    // phase mask on local bits
+    uint64_t zo;    // phase mask on qubits outside the tile
+    uint32_t hb;    // highest local bit of xl: each pair is visited with it clear
+    uint32_t im;    // Im(conj(a_s) a_{s^x}) instead of Re
+    double factor;  // +-2 (i^{nY} and (-1)^{|x & z|} folded in)
+};
+struct PauliTilePass {
+    uint32_t K, l, m, nterms;
+    uint8_t hq[16];
+    PauliTileTerm t[kMaxTerms];
+};
+// Tile size of the pass kernel (32 KiB of shared memory: several CTAs per SM
+// overlap one tile's loads with another's arithmetic).
+template <class T> constexpr int pauli_tile_bits() { return sizeof(T) == 4 ? 12 : 11; }
+template <class T>
+cudaError_t launch_pauli_tile(const void *st, uint32_t n, bool ff_resident, const PauliTilePass &p,
+                              const ReduceScratch &rs, cudaStream_t s);
+
 // dump: support counts per block, then compaction.
 struct DumpSpec {
     uint32_t nq;

@@ -8,6 +8,7 @@
 // double per thread before the block tree.
 #include <float.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/kbwg.h"
@@ -520,6 +521,156 @@ cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, 
     return cudaGetLastError();
 }
 
+// ---- tiled pass over many pair-form strings ---------------------------------------
+// One tile of 2^K amplitudes per CTA iteration, staged in shared memory with
+// coalesced loads (chunks of 2^l contiguous amplitudes); every term then
+// visits its 2^(K-1) pairs inside the tile.  complex64: exact float products
+// summed in float-float (AccF) per thread.  complex128: the tile is held in
+// float-float form (binary64 split on load, or the float-float resident
+// form as is), each pair product is a float-float dot product, summed per
+// tile in float-float and added to a binary64 accumulator once per tile.
+template <class T> struct TileVal;
+template <> struct TileVal<float> {
+    using V = cx<float>;
+};
+template <> struct TileVal<double> {
+    struct V {
+        ff::f2 re, im;
+    };
+};
+
+__device__ __forceinline__ uint64_t tile_base_of(uint64_t tau, uint32_t l, uint32_t m, const uint8_t *hq) {
+    uint64_t b = tau << l;
+    for (uint32_t j = 0; j < m; j++) b = insert_zero(b, hq[j]);
+    return b;
+}
+
+template <class T, bool kFF>
+__global__ void __launch_bounds__(256) k_pauli_tile(const void *__restrict__ st, uint32_t n,
+                                                    const __grid_constant__ PauliTilePass p, ReduceScratch rs) {
+    using V = typename TileVal<T>::V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *tile = reinterpret_cast<V *>(smem_raw);
+    const uint32_t K = p.K, l = p.l, m = p.m, nt = p.nterms;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(smem_raw + (sizeof(V) << K));
+    for (uint32_t c = threadIdx.x; c < (1u << m); c += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
+        chunk_off[c] = off;
+    }
+    const uint64_t tiles = 1ull << (n - K);
+    const uint32_t lowmask = (1u << l) - 1u;
+    const uint32_t npairs = 1u << (K - 1);
+    typename AccOf<T>::type acc[kMaxTerms];
+    __syncthreads();
+    for (uint64_t tau = blockIdx.x; tau < tiles; tau += gridDim.x) {
+        const uint64_t base = tile_base_of(tau, l, m, p.hq);
+        for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x) {
+            const uint64_t gidx = base + chunk_off[u >> l] + (u & lowmask);
+            if constexpr (sizeof(T) == 4) {
+                tile[u] = reinterpret_cast<const cx<float> *>(st)[gidx];
+            } else if constexpr (kFF) {
+                const float4 f = reinterpret_cast<const float4 *>(st)[gidx];  // re.hi, im.hi, re.lo, im.lo
+                tile[u] = V{ff::f2{f.x, f.z}, ff::f2{f.y, f.w}};
+            } else {
+                const cx<double> a = reinterpret_cast<const cx<double> *>(st)[gidx];
+                tile[u] = V{ff::from_double(a.re), ff::from_double(a.im)};
+            }
+        }
+        __syncthreads();
+        // (not unrolled: one copy of the pair loop; acc[] lives in local
+        // memory, touched once per term and tile)
+#pragma unroll 1
+        for (int k = 0; k < (int)nt; k++) {
+            const PauliTileTerm &t = p.t[k];
+            const uint32_t tile_par = (uint32_t)__popcll(base & t.zo) & 1u;
+            // four independent partial sums per thread (the pair products are
+            // independent; one running sum would serialise its rounding chain)
+            constexpr int U = 4;
+            if constexpr (sizeof(T) == 4) {
+                AccF part[U];
+                for (uint32_t q0 = threadIdx.x; q0 < npairs; q0 += U * blockDim.x) {
+#pragma unroll
+                    for (int j = 0; j < U; j++) {
+                        const uint32_t q = q0 + j * blockDim.x;
+                        if (q >= npairs) break;
+                        const uint32_t u = (uint32_t)insert_zero(q, t.hb);
+                        const cx<float> a = tile[u], b = tile[u ^ t.xl];
+                        const bool neg = ((__popc(u & t.zl) & 1u) ^ tile_par) != 0;
+                        if (!t.im) {  // Re(conj(a) b) = a.re b.re + a.im b.im
+                            if (neg) {
+                                part[j].add_prod_neg(a.re, b.re);
+                                part[j].add_prod_neg(a.im, b.im);
+                            } else {
+                                part[j].add_prod(a.re, b.re);
+                                part[j].add_prod(a.im, b.im);
+                            }
+                        } else {  // Im(conj(a) b) = a.re b.im - a.im b.re
+                            if (neg) {
+                                part[j].add_prod_neg(a.re, b.im);
+                                part[j].add_prod(a.im, b.re);
+                            } else {
+                                part[j].add_prod(a.re, b.im);
+                                part[j].add_prod_neg(a.im, b.re);
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < U; j++) acc[k].add2(part[j].hi, part[j].lo);
+            } else {
+                ff::f2 part[U];
+#pragma unroll
+                for (int j = 0; j < U; j++) part[j] = ff::f2{0.f, 0.f};
+                for (uint32_t q0 = threadIdx.x; q0 < npairs; q0 += U * blockDim.x) {
+#pragma unroll
+                    for (int j = 0; j < U; j++) {
+                        const uint32_t q = q0 + j * blockDim.x;
+                        if (q >= npairs) break;
+                        const uint32_t u = (uint32_t)insert_zero(q, t.hb);
+                        const V a = tile[u], b = tile[u ^ t.xl];
+                        const ff::f2 v =
+                            t.im ? ff::dot2(a.re, b.im, ff::neg(a.im), b.re) : ff::dot2(a.re, b.re, a.im, b.im);
+                        const bool neg = ((__popc(u & t.zl) & 1u) ^ tile_par) != 0;
+                        part[j] = neg ? ff::sub(part[j], v) : ff::add(part[j], v);
+                    }
+                }
+                const ff::f2 sum = ff::add(ff::add(part[0], part[1]), ff::add(part[2], part[3]));
+                acc[k].v += (double)sum.h + (double)sum.l;
+            }
+        }
+        __syncthreads();
+    }
+    for (int k = 0; k < (int)nt; k++) {
+        {
+            const double v = block_sum(acc[k].value() * p.t[k].factor);
+            if (threadIdx.x == 0) rs.partials[(size_t)blockIdx.x * kMaxTerms + k] = v;
+        }
+    }
+    if (last_block(rs.ticket)) {
+        for (int k = 0; k < (int)nt; k++) {
+            const double tsum = sum_partials(rs.partials, gridDim.x, kMaxTerms, k);
+            if (threadIdx.x == 0) rs.result[k] = tsum;
+        }
+        if (threadIdx.x == 0) *rs.ticket = 0;
+    }
+}
+
+template <class T>
+cudaError_t launch_pauli_tile(const void *st, uint32_t n, bool ff_resident, const PauliTilePass &p,
+                              const ReduceScratch &rs, cudaStream_t s) {
+    using V = typename TileVal<T>::V;
+    const size_t smem = (sizeof(V) << p.K) + (sizeof(uint64_t) << p.m);
+    auto kern = (sizeof(T) == 8 && ff_resident) ? k_pauli_tile<T, true> : k_pauli_tile<T, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = 1ull << (n - p.K);
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)kReduceBlocks);
+    kern<<<grid, 256, smem, s>>>(st, n, p, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ---- support test for dump / sample ---------------------------------------
 // Reference: hypot(re, im) > F(eps) in F (src/dense.rs:374).  With hypot
 // correctly rounded this is re^2 + im^2 > m^2, m the midpoint between F(eps)
@@ -810,6 +961,8 @@ namespace kbwg {
                                             cudaStream_t);                                                    \
     template cudaError_t launch_pauli_group<T>(const void *, uint32_t, const PauliGroup &, const ReduceScratch &, \
                                                cudaStream_t);                                                 \
+    template cudaError_t launch_pauli_tile<T>(const void *, uint32_t, bool, const PauliTilePass &,               \
+                                              const ReduceScratch &, cudaStream_t);                           \
     template cudaError_t launch_dump_count<T>(const void *, uint32_t, uint64_t *, cudaStream_t);               \
     template cudaError_t launch_dump_write<T>(const void *, uint32_t, const uint64_t *, const DumpSpec &,        \
                                               uint64_t *, double *, double *, cudaStream_t);                  \

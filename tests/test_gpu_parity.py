@@ -220,6 +220,28 @@ def test_exp_value(prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+def test_exp_value_tiled_passes(prec):
+    """Strings with flip masks go through tiled passes (many masks per pass);
+    strings too wide for one tile fall back to one pass per mask.  Mixes X/Y
+    strings on low, high and scattered qubits with Z factors inside and
+    outside the tile."""
+    n = 17
+    sim, ref = both(n, C.hea(n, 2, C.hea_params(n, 2, 91)), prec)
+    rng = np.random.default_rng(92)
+    h = C.tfim_ring(n)
+    for _ in range(40):
+        k = int(rng.integers(1, 5))
+        qs = rng.choice(n, size=k, replace=False)
+        h.append((float(rng.normal()), [(int(rng.integers(1, 4)), int(q)) for q in qs]))
+    h.append((0.7, [(C.PAULI_X, q) for q in range(5, 16)]))            # 11 high flip bits: no tile holds it
+    h.append((-0.4, [(C.PAULI_Y, q) for q in (0, 6, 9, 12, 13, 14, 15, 16)]))
+    tol = 1e-11 if prec == "c128" else 2e-5
+    assert abs(sim.exp_value(h) - ref.exp_value(h)) < tol * len(h)
+    for term in h[-6:]:
+        assert abs(sim.exp_value([term]) - ref.exp_value([term])) < tol
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_swap_qubits_exact(prec):
     n = 15
     circ = C.random_circuit(n, 100, 77, max_controls=2)
