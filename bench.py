@@ -309,6 +309,47 @@ def run_adjoint_large(args, torch, DenseGB300, C):
                         "abs_dE_c64_vs_c128": abs(res["c64"][0] - res["c128_ff"][0])}}
 
 
+def run_grover_bench(args, torch, DenseGB300, C):
+    """The reference's CPU-runnable case: plain Grover search, 12 qubits,
+    complex128, 50 iterations (2,962 gates), marked index seeded in
+    [0, 4096); output the probability vector (dump of all qubits) and 1024
+    samples from injected draws.  Latency-bound: wall time per run through the
+    C ABI against the restated Dense<f64> on the host, and the success
+    probability against its closed form."""
+    import oracle
+    n, it, seeds = 12, 50, 10
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    qs = list(range(n))[::-1]  # dump packs qubits[0] as the most significant bit: natural index order
+
+    def run(target, seed):
+        marked = C.grover_marked(seed)
+        target.clear()
+        target.apply(C.grover(n, marked, it))
+        st, re, im = target.dump(qs)
+        hist = target.sample(qs, 1024, C.uniform_draws(1024, seed))
+        p = float(np.sum((re * re + im * im)[st == marked]))
+        return p, hist
+
+    run(sim, 0)
+    run(sim, 1)  # second sight of the structure builds its replay graph
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = [run(sim, sd) for sd in range(seeds)]
+    torch.cuda.synchronize()
+    t_gpu = (time.perf_counter() - t0) / seeds
+    o = oracle.OracleDense(n, "c128")
+    t0 = time.perf_counter()
+    ref = [run(o, sd) for sd in range(2)]
+    t_cpu = (time.perf_counter() - t0) / 2
+    same = all(np.array_equal(res[i][1][0], ref[i][1][0]) and np.array_equal(res[i][1][1], ref[i][1][1])
+               for i in range(2))
+    sim.close()
+    return {"config": "grover-12q-50it-c128 (probabilities + 1024 samples)", "ms_per_run": round(t_gpu * 1e3, 3),
+            "cpu_port_ms_per_run": round(t_cpu * 1e3, 3), "cpu_threads": oracle.num_threads(),
+            "success_probability": res[0][0], "closed_form": C.grover_success_probability(n, it),
+            "samples_identical_to_oracle": bool(same)}
+
+
 def run_batch_bench(args, torch, C):
     """Batched forward: 4096 hardware-efficient-ansatz circuits (n ~ U{8..20},
     L ~ U{2..8}) in one persistent launch; circuits/s and the max |dE| of the
@@ -482,6 +523,8 @@ def run_ours(args, world, rank, local):
         secondary["adjoint_large"] = run_adjoint_large(args, torch, DenseGB300, C)
     if args.batch:
         secondary["batch"] = run_batch_bench(args, torch, C)
+    if args.grover:
+        secondary["grover"] = run_grover_bench(args, torch, DenseGB300, C)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -530,6 +573,7 @@ def main():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--no-adjoint-large", dest="adjoint_large", action="store_false")
+    ap.add_argument("--no-grover", dest="grover", action="store_false")
     ap.add_argument("--adj-large-qubits", type=int, default=32)
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-reps", type=int, default=3)

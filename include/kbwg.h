@@ -64,9 +64,11 @@ enum { KBWG_PAULI_X = 1, KBWG_PAULI_Y = 2, KBWG_PAULI_Z = 3 };
 /* creation flags */
 enum {
     KBWG_FLAG_NO_FUSION = 1u << 0, /* run one kernel per gate (debug / A-B timing) */
-    KBWG_FLAG_FAST_C128 = 1u << 1, /* complex128 gate arithmetic in float-float (see DESIGN) */
-    KBWG_FLAG_EXACT_ORDER = 1u << 2 /* fuse without reordering commuting gates: amplitudes then
-                                       equal the reference's bit for bit */
+    KBWG_FLAG_FAST_C128 = 1u << 1, /* complex128 gates in float-float arithmetic (pairs of floats,
+                                      ~48-bit significand, < 1e-12 relative to binary64) */
+    KBWG_FLAG_EXACT_ORDER = 1u << 2, /* fuse without reordering commuting gates: amplitudes then
+                                        equal the reference's bit for bit */
+    KBWG_FLAG_NO_GRAPHS = 1u << 3    /* do not replay repeated gate structures from CUDA graphs */
 };
 
 /* QuantumExecution::new (src/quantum_execution.rs:53; src/dense.rs:70-89).

@@ -15,6 +15,7 @@ C64, C128 = 0, 1
 FLAG_NO_FUSION = 1
 FLAG_FAST_C128 = 2
 FLAG_EXACT_ORDER = 4
+FLAG_NO_GRAPHS = 8
 
 
 class KbwgError(RuntimeError):

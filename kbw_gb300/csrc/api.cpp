@@ -253,6 +253,7 @@ int32_t kbwg_free(kbwg_sim *s) {
     s->tmp4.release();
     s->tmp5.release();
     s->prof.release();
+    release_graphs(*s);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return KBWG_OK;

@@ -68,6 +68,7 @@ struct Sim {
     uint64_t rng = 0;  // splitmix64 state of the handle's own draw generator
 
     Profiler prof;
+    void *graphs = nullptr;  // replay cache of planned sweeps (sweep.cu)
 
     // statistics of the last flush
     uint64_t last_passes = 0;
@@ -81,6 +82,8 @@ bool ff_capable(const Sim &s);
 cudaError_t ensure_binary64(Sim &s);
 // |0...0> in the handle's resident format.
 cudaError_t init_state(Sim &s);
+// Free the replay cache of planned sweeps.
+void release_graphs(Sim &s);
 
 // Build the descriptor of one trait gate: constants computed in the state
 // precision exactly as kbw Dense<F> does (src/dense.rs:211-334).

@@ -147,6 +147,76 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, 2)
     }
 }
 
+// ---- replay cache ------------------------------------------------------------------
+// A flush whose gate structure (kinds, targets and controls, after the
+// float-float rewrite) matches an earlier flush of the handle reuses that
+// flush's plan, its device program buffer and an instantiated CUDA graph of
+// its sweep launches: only the gate constants are re-packed and uploaded.
+// Parameter sweeps (VQE, parameter shift) and repeated circuits skip the
+// planner and the per-launch host overhead.
+struct SweepGraph {
+    const void *kernel = nullptr;   // which k_sweep instantiation
+    std::vector<uint64_t> sig;      // structure of the flushed gate list
+    std::vector<uint32_t> src;      // program slot -> index in the flushed list
+    std::vector<TileGate> planned;  // program with unpacked constants
+    void *dprog = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    size_t sweeps = 0;
+    uint64_t last_use = 0;
+};
+struct GraphCache {
+    std::vector<SweepGraph> entries;
+    std::vector<uint64_t> seen;  // structure hashes flushed once (a graph is built on the second time)
+    uint64_t clock = 0;
+};
+constexpr size_t kGraphCacheEntries = 8;
+
+static void free_entry(SweepGraph &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.dprog) cudaFree(g.dprog);
+    g.exec = nullptr;
+    g.dprog = nullptr;
+}
+
+void release_graphs(Sim &s) {
+    GraphCache *c = (GraphCache *)s.graphs;
+    if (!c) return;
+    for (SweepGraph &g : c->entries) free_entry(g);
+    delete c;
+    s.graphs = nullptr;
+}
+
+static uint64_t hash_of(const std::vector<uint64_t> &sig) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the words
+    for (uint64_t w : sig) {
+        h ^= w;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+static std::vector<uint64_t> structure_of(const GateDesc *gates, size_t count) {
+    std::vector<uint64_t> sig(2 * count);
+    for (size_t i = 0; i < count; i++) {
+        sig[2 * i] = (uint64_t)gates[i].kind | ((uint64_t)gates[i].target << 8);
+        sig[2 * i + 1] = gates[i].ctrl;
+    }
+    return sig;
+}
+
+// Pack the planned program with the constants of `gates` and upload it.
+template <class P>
+static cudaError_t upload_program(Sim &s, const std::vector<TileGate> &planned, const std::vector<uint32_t> &src,
+                                  const GateDesc *gates, void *dst) {
+    std::vector<TileGate> prog = planned;
+    for (size_t i = 0; i < prog.size(); i++) {
+        memcpy(prog[i].c, gates[src[i]].c, sizeof prog[i].c);
+        P::pack_host(prog[i]);
+    }
+    // pageable source: the call returns once the host buffer is consumed
+    return copy_async(dst, prog.data(), prog.size() * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
+}
+
 template <class P, int K, int R>
 static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     using SK = SweepKernel<P, K, R>;
@@ -164,22 +234,69 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    const void *kid = (const void *)k_sweep<P, K, R>;
+    // timed profiling marks every launch with events, which a graph replay cannot
+    bool graphs = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
+    std::vector<uint64_t> sig;
+    if (graphs) {
+        if (!s.graphs) s.graphs = new GraphCache();
+        GraphCache &gc = *(GraphCache *)s.graphs;
+        sig = structure_of(gates, count);
+        sig.push_back((uint64_t)(uintptr_t)kid);
+        const uint64_t h = hash_of(sig);
+        bool again = false;
+        for (uint64_t x : gc.seen) again = again || x == h;
+        if (!again) {  // first sight of this structure: launch directly, remember it
+            if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
+            gc.seen.push_back(h);
+            graphs = false;
+        }
+        for (SweepGraph &g : gc.entries) {
+            if (g.kernel != kid || g.sig != sig) continue;
+            cudaError_t e = upload_program<P>(s, g.planned, g.src, gates, g.dprog);
+            if (e != cudaSuccess) return e;
+            e = cudaGraphLaunch(g.exec, s.stream);
+            if (e != cudaSuccess) return e;
+            for (size_t i = 0; i < g.sweeps; i++) count_launch();
+            g.last_use = ++gc.clock;
+            s.last_passes = g.sweeps;
+            return cudaSuccess;
+        }
+    }
     std::vector<PlannedSweep> plan =
         plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0);
-    size_t total = 0;
-    for (const PlannedSweep &sw : plan) total += sw.gates.size();
-    std::vector<TileGate> prog;
-    prog.reserve(total);
-    for (const PlannedSweep &sw : plan) prog.insert(prog.end(), sw.gates.begin(), sw.gates.end());
-    for (TileGate &t : prog) P::pack_host(t);
-    cudaError_t e = s.tmp4.ensure(total * sizeof(TileGate));
-    if (e != cudaSuccess) return e;
-    // pageable source: the call returns once the host buffer is consumed
-    e = copy_async(s.tmp4.ptr, prog.data(), total * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
-    if (e != cudaSuccess) return e;
-    const TileGate *dprog = (const TileGate *)s.tmp4.ptr;
+    std::vector<TileGate> planned;
+    std::vector<uint32_t> src;
+    for (const PlannedSweep &sw : plan) {
+        planned.insert(planned.end(), sw.gates.begin(), sw.gates.end());
+        src.insert(src.end(), sw.src.begin(), sw.src.end());
+    }
+    const size_t total = planned.size();
+    void *dbuf = nullptr;
+    cudaError_t e;
+    if (graphs) {
+        e = cudaMalloc(&dbuf, std::max<size_t>(total, 1) * sizeof(TileGate));
+        if (e != cudaSuccess) return e;
+    } else {
+        e = s.tmp4.ensure(total * sizeof(TileGate));
+        if (e != cudaSuccess) return e;
+        dbuf = s.tmp4.ptr;
+    }
+    e = upload_program<P>(s, planned, src, gates, dbuf);
+    if (e != cudaSuccess) {
+        if (graphs) cudaFree(dbuf);
+        return e;
+    }
+    const TileGate *dprog = (const TileGate *)dbuf;
     const uint64_t tiles = 1ull << (s.n - K);
     const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * 2);
+    if (graphs) {
+        e = cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaFree(dbuf);
+            return e;
+        }
+    }
     size_t off = 0;
     for (const PlannedSweep &sw : plan) {
         SweepParams p;
@@ -200,15 +317,49 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         off += sw.gates.size();
         if (s.prof.on) s.prof.mark(s.stream);
         k_sweep<P, K, R><<<(unsigned)grid, SK::kThreads, SK::kSmem, s.stream>>>((Mem *)s.state, p);
-        count_launch();
+        if (!graphs) count_launch();
         e = cudaGetLastError();
         if (s.prof.on) {
             s.prof.mark(s.stream);
             s.prof.bytes += 2.0 * (double)s.elem * (double)s.ns;
         }
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess) break;
     }
     s.last_passes = plan.size();
+    if (!graphs) return e;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s.stream, &graph);
+    if (e == cudaSuccess) e = ec;
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, s.stream);
+    if (e != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaStreamSynchronize(s.stream);
+        cudaFree(dbuf);
+        return e;
+    }
+    for (size_t i = 0; i < plan.size(); i++) count_launch();
+    GraphCache &gc = *(GraphCache *)s.graphs;
+    if (gc.entries.size() >= kGraphCacheEntries) {  // evict the least recently used
+        size_t lru = 0;
+        for (size_t i = 1; i < gc.entries.size(); i++)
+            if (gc.entries[i].last_use < gc.entries[lru].last_use) lru = i;
+        cudaStreamSynchronize(s.stream);  // its program buffer may still be read
+        free_entry(gc.entries[lru]);
+        gc.entries.erase(gc.entries.begin() + (long)lru);
+    }
+    SweepGraph g;
+    g.kernel = kid;
+    g.sig = std::move(sig);
+    g.src = std::move(src);
+    g.planned = std::move(planned);
+    g.dprog = dbuf;
+    g.exec = exec;
+    g.sweeps = plan.size();
+    g.last_use = ++gc.clock;
+    gc.entries.push_back(std::move(g));
     return cudaSuccess;
 }
 

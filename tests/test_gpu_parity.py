@@ -425,3 +425,30 @@ def test_fast_c128_distance_and_gradient_after_gates():
     assert np.max(np.abs(g_a - g_b)) < 1e-10
     # the adjoint leaves |0...0>
     assert abs(a.state()[0] - 1.0) < 1e-15
+
+
+@pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", True), ("c128", False)])
+def test_graph_replay_same_structure_new_angles(prec, fast):
+    """Repeated flushes of one gate structure replay a CUDA graph with freshly
+    uploaded constants: every repetition (other angles, from |0>) must match
+    the oracle and a handle that never uses graphs."""
+    import kbw_gb300._native as N
+    n = 16
+    a = DenseGB300(n, prec, fast_c128=fast)
+    b = DenseGB300(n, prec, fast_c128=fast, graphs=False)
+    tol = 1e-12 if prec == "c128" else 1e-5
+    for rep in range(4):
+        # same structure every repetition (brickwork seed fixed), new angles
+        circ = C.hea(n, 3, C.hea_params(n, 3, 100 + rep)) + [(k, t, c, 0.1 * rep + 0.3 * i)
+                                                            for i, (k, t, c, _) in enumerate(C.brickwork(n, 2, 200))]
+        a.clear()
+        b.clear()
+        l0 = N.launch_count()
+        a.apply(circ)
+        a.flush()
+        assert N.launch_count() - l0 == a.last_flush_stats()[1]
+        b.apply(circ)
+        ref = oracle.OracleDense(n, prec)
+        ref.apply(circ)
+        assert rel_err(a.state(), ref.state()) < tol
+        assert rel_err(a.state(), b.state()) < tol
