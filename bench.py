@@ -350,6 +350,41 @@ def run_grover_bench(args, torch, DenseGB300, C):
             "samples_identical_to_oracle": bool(same)}
 
 
+def run_gate_classes(args):
+    """Per gate class: CUDA-event time of the sweeps that apply 32 gates of
+    one class (first row: a single RZ, the memory-pass floor of a sweep);
+    us_per_gate = sweep time / gates."""
+    from kbw_gb300 import DenseGB300
+    from kbw_gb300 import circuits as C
+    n, prec = args.qubits, args.prec
+    sim = DenseGB300(n, prec, fast_c128=(prec == "c128" and args.arith == "ff"))
+    cases = [("one RZ (memory pass)", [(C.RZ, 3, (), 0.3)]),
+             ("32 RY on a register qubit", [(C.RY, 8, (), 0.1 * i) for i in range(32)]),
+             ("32 RX on a register qubit", [(C.RX, 8, (), 0.1 * i) for i in range(32)]),
+             ("32 H on qubits 6..9", [(C.H, 6 + i % 4, (), 0.0) for i in range(32)]),
+             ("32 RZ on a register qubit", [(C.RZ, 8, (), 0.1 * i) for i in range(32)]),
+             ("32 P on a register qubit", [(C.P, 8, (), 0.1 * i) for i in range(32)]),
+             ("32 Z on a register qubit", [(C.Z, 8, (), 0.0)] * 32),
+             ("32 X on a lane qubit", [(C.X, 2, (), 0.0)] * 32),
+             ("32 RY on a lane qubit", [(C.RY, 2, (), 0.1 * i) for i in range(32)]),
+             ("32 CNOT 7->8 (register control)", [(C.X, 8, (7,), 0.0)] * 32),
+             ("brickwork 13 qubits, 3 layers", C.brickwork(13, 3, 0))]
+    out = []
+    for name, circ in cases:
+        sim.apply(circ)
+        sim.flush()
+        sim.profile(True)
+        for _ in range(3):
+            sim.apply(circ)
+            sim.flush()
+        nl, ms, b = sim.profile_read()
+        sim.profile(False)
+        out.append({"case": name, "gates": len(circ), "sweeps": nl // 3, "ms_per_rep": round(ms / 3, 4),
+                    "us_per_gate": round(1000 * ms / 3 / len(circ), 3)})
+    sim.close()
+    return out
+
+
 def run_batch_bench(args, torch, C):
     """Batched forward: 4096 hardware-efficient-ansatz circuits (n ~ U{8..20},
     L ~ U{2..8}) in one persistent launch; circuits/s and the max |dE| of the
@@ -574,6 +609,8 @@ def main():
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--no-adjoint-large", dest="adjoint_large", action="store_false")
     ap.add_argument("--no-grover", dest="grover", action="store_false")
+    ap.add_argument("--gate-classes", action="store_true",
+                    help="instead of the benchmark: per gate class sweep times on --qubits/--prec/--arith")
     ap.add_argument("--adj-large-qubits", type=int, default=32)
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-reps", type=int, default=3)
@@ -586,6 +623,12 @@ def main():
                          "of k_sweep<FF2> (1017.4 MB) scaled by the amplitude count")
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.gate_classes:
+        import kbw_gb300
+        kbw_gb300.load()
+        for row in run_gate_classes(args):
+            print(json.dumps(row), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
