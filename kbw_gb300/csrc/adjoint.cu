@@ -75,6 +75,74 @@ __global__ void __launch_bounds__(256) k_apply_group(const cx<T> *__restrict__ p
     }
 }
 
+// lambda (+)= H phi for every string of one tiled pass (the strings' flip
+// masks lie in the tile): the phi tile is staged in shared memory with
+// coalesced loads, then each thread sums, for the amplitudes it owns, the
+// terms c_k i^{ny_k} (-1)^{|src & z_k|} phi_src, src = s ^ x_k.
+struct ApplyTileTerm {
+    uint32_t xl, zl;  // flip and phase masks on local bits
+    uint64_t zo;      // phase mask on qubits outside the tile
+    double cre, cim;  // c_k * i^{ny_k}
+};
+struct ApplyTilePass {
+    uint32_t K, l, m, nterms, init;
+    uint8_t hq[16];
+    ApplyTileTerm t[kMaxTerms];
+};
+constexpr int kApplyTileBits = 11;  // 2^11 amplitudes (16/32 KiB) per tile
+
+template <class T>
+__global__ void __launch_bounds__(256) k_apply_tile(const cx<T> *__restrict__ phi, cx<T> *__restrict__ lam, uint32_t n,
+                                                    const __grid_constant__ ApplyTilePass p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T cre[kMaxTerms], cim[kMaxTerms];  // coefficients converted once (no per-term F2F)
+    cx<T> *tile = reinterpret_cast<cx<T> *>(smem_raw);
+    const uint32_t K = p.K, l = p.l, m = p.m;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(smem_raw + (sizeof(cx<T>) << K));
+    if (threadIdx.x < kMaxTerms) {
+        cre[threadIdx.x] = (T)p.t[threadIdx.x].cre;
+        cim[threadIdx.x] = (T)p.t[threadIdx.x].cim;
+    }
+    for (uint32_t c = threadIdx.x; c < (1u << m); c += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
+        chunk_off[c] = off;
+    }
+    const uint64_t tiles = 1ull << (n - K);
+    const uint32_t lowmask = (1u << l) - 1u;
+    __syncthreads();
+    for (uint64_t tau = blockIdx.x; tau < tiles; tau += gridDim.x) {
+        uint64_t base = tau << l;
+        for (uint32_t j = 0; j < m; j++) {
+            const uint64_t low = (1ull << p.hq[j]) - 1;
+            base = ((base & ~low) << 1) | (base & low);
+        }
+        for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x)
+            tile[u] = phi[base + chunk_off[u >> l] + (u & lowmask)];
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x) {
+            T ar = 0, ai = 0;
+            for (uint32_t k = 0; k < p.nterms; k++) {
+                const ApplyTileTerm &t = p.t[k];
+                const uint32_t src = u ^ t.xl;
+                const bool neg = ((__popc(src & t.zl) + __popcll(base & t.zo)) & 1) != 0;
+                const T wr = neg ? -cre[k] : cre[k], wi = neg ? -cim[k] : cim[k];
+                const cx<T> a = tile[src];
+                ar += wr * a.re - wi * a.im;
+                ai += wr * a.im + wi * a.re;
+            }
+            const uint64_t gidx = base + chunk_off[u >> l] + (u & lowmask);
+            if (!p.init) {
+                const cx<T> o = lam[gidx];
+                ar += o.re;
+                ai += o.im;
+            }
+            lam[gidx] = cx<T>{ar, ai};
+        }
+        __syncthreads();
+    }
+}
+
 // Re<a|b> (FP64-grade) into result[0].
 template <class T>
 __global__ void __launch_bounds__(256) k_inner_re(const cx<T> *__restrict__ a, const cx<T> *__restrict__ b,
@@ -536,10 +604,60 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        // the program/meta buffers are reused by the next sweep: wait for this one
-        e = cudaStreamSynchronize(s.stream);
+        // (the next sweep's uploads into prog/meta are stream-ordered after this
+        // sweep's kernels: no host synchronisation needed)
+    }
+    return cudaSuccess;
+}
+
+// lambda = H phi in tiled passes (ring TFIM at 24 qubits: 3 passes instead
+// of one per flip mask); strings too wide for a tile fall back to one pass
+// per flip mask.
+template <class T>
+static cudaError_t apply_hamiltonian_tiled(Sim &s, void *lam, const std::vector<PauliString> &H, bool &done) {
+    done = false;
+    const int K = kApplyTileBits;
+    if (s.n < (uint32_t)K + 1 || H.empty()) return cudaSuccess;
+    std::vector<uint64_t> xm;
+    for (const PauliString &t : H) xm.push_back(t.x);
+    std::vector<size_t> wide;
+    const std::vector<PauliPass> passes = plan_pauli_passes(s.n, K, xm, kMaxTerms, wide);
+    if (!wide.empty()) return cudaSuccess;
+    const size_t smem = (sizeof(cx<T>) << K) + (sizeof(uint64_t) << (K - kLaneBits));
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_apply_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint64_t tiles = 1ull << (s.n - K);
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, 152ull * 8);
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const PauliPass &pp = passes[pi];
+        ApplyTilePass a;
+        memset(&a, 0, sizeof a);
+        a.K = (uint32_t)K;
+        a.l = pp.l;
+        a.m = pp.m;
+        a.init = pi == 0 ? 1u : 0u;
+        memcpy(a.hq, pp.hq, sizeof a.hq);
+        for (size_t j = 0; j < pp.members.size(); j++) {
+            const PauliString &t = H[pp.members[j]];
+            ApplyTileTerm &tt = a.t[j];
+            tt.xl = pp.local(t.x);
+            tt.zl = pp.local(t.z & pp.tile_mask);
+            tt.zo = t.z & ~pp.tile_mask;
+            const int q = t.ny & 3;  // i^ny
+            tt.cre = (q == 0) ? t.coef : (q == 2 ? -t.coef : 0.0);
+            tt.cim = (q == 1) ? t.coef : (q == 3 ? -t.coef : 0.0);
+        }
+        a.nterms = (uint32_t)pp.members.size();
+        k_apply_tile<T><<<grid, 256, smem, s.stream>>>((const cx<T> *)s.state, (cx<T> *)lam, s.n, a);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    done = true;
     return cudaSuccess;
 }
 
@@ -660,7 +778,9 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         }
     }
     // 2. lambda = H phi, E = Re<phi|lambda>
-    e = apply_hamiltonian<T>(s, bufs.lam, make_groups(H));
+    bool tiled = false;
+    e = apply_hamiltonian_tiled<T>(s, bufs.lam, H, tiled);
+    if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, bufs.lam, make_groups(H));
     if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
     e = inner_re<T>(s, s.state, bufs.lam, energy);
     if (e != cudaSuccess) return fail_cuda(e, "energy");

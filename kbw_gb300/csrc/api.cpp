@@ -599,55 +599,36 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
     // strings with a flip mask: tiled passes, each covering every string whose
     // flip mask fits one tile (ring TFIM, 30 qubits: 4 passes instead of 30)
     const int K = s->prec ? pauli_tile_bits<double>() : pauli_tile_bits<float>();
-    auto low_bits = [&](uint64_t need) {  // largest contiguous low block with the rest of `need` above it
-        for (int l = K; l >= 5; l--) {
-            const uint64_t above = need & ~((1ull << l) - 1);
-            if (l + __builtin_popcountll(above) <= K) return l;
-        }
-        return -1;
-    };
     const bool tiled = s->n >= (uint32_t)K;
-    auto by_tiles = [&](const PauliString &t) { return tiled && t.x != 0 && low_bits(t.x) >= 0; };
+    std::vector<char> by_tile(n_strings, 0);
     if (tiled) {
-        std::vector<size_t> pend;
+        std::vector<size_t> pair_idx;
+        std::vector<uint64_t> xm;
         for (size_t k = 0; k < n_strings; k++)
-            if (by_tiles(strs[order[k]])) pend.push_back(order[k]);
-        while (!pend.empty()) {
+            if (strs[order[k]].x != 0) {
+                pair_idx.push_back(order[k]);
+                xm.push_back(strs[order[k]].x);
+            }
+        std::vector<size_t> wide;
+        for (const PauliPass &pp : plan_pauli_passes(s->n, K, xm, kMaxTerms, wide)) {
             PauliTilePass pass;
             memset(&pass, 0, sizeof pass);
-            uint64_t needed = 0;
-            std::vector<size_t> take, rest;
-            for (size_t k : pend) {
-                const uint64_t nn = needed | strs[k].x;
-                if (take.size() < (size_t)kMaxTerms && low_bits(nn) >= 0) {
-                    needed = nn;
-                    take.push_back(k);
-                } else {
-                    rest.push_back(k);
-                }
-            }
-            const int l = low_bits(needed);
-            uint64_t h = needed & ~((1ull << l) - 1);
-            for (uint32_t q = (uint32_t)l; q < s->n && l + __builtin_popcountll(h) < K; q++) h |= 1ull << q;
             pass.K = (uint32_t)K;
-            pass.l = (uint32_t)l;
-            for (uint32_t q = 0; q < 64; q++)
-                if (h >> q & 1) pass.hq[pass.m++] = (uint8_t)q;
-            const uint64_t tile_mask = ((1ull << l) - 1) | h;
-            auto local = [&](uint64_t mask) {
-                uint32_t r = (uint32_t)(mask & ((1ull << l) - 1));
-                for (uint32_t j = 0; j < pass.m; j++)
-                    if (mask >> pass.hq[j] & 1) r |= 1u << (l + j);
-                return r;
-            };
-            for (size_t j = 0; j < take.size(); j++) {
-                const PauliString &t = strs[take[j]];
+            pass.l = pp.l;
+            pass.m = pp.m;
+            memcpy(pass.hq, pp.hq, sizeof pass.hq);
+            std::vector<size_t> take;
+            for (size_t j = 0; j < pp.members.size(); j++) {
+                const size_t k = pair_idx[pp.members[j]];
+                const PauliString &t = strs[k];
                 PauliTileTerm &tt = pass.t[j];
-                tt.xl = local(t.x);
+                tt.xl = pp.local(t.x);
                 tt.hb = 31 - __builtin_clz(tt.xl);
-                tt.zl = local(t.z & tile_mask);
-                tt.zo = t.z & ~tile_mask;
+                tt.zl = pp.local(t.z & pp.tile_mask);
+                tt.zo = t.z & ~pp.tile_mask;
                 pair_term(t, tt.factor, tt.im);
+                take.push_back(k);
+                by_tile[k] = 1;
             }
             pass.nterms = (uint32_t)take.size();
             CUDA_TRY(dispatch(s, [&](auto *tp) {
@@ -657,11 +638,10 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
             CUDA_TRY(cudaMemcpyAsync(d_vals + slot_of.size(), s->rs.result, take.size() * 8,
                                      cudaMemcpyDeviceToDevice, s->stream));
             slot_of.insert(slot_of.end(), take.begin(), take.end());
-            pend.swap(rest);
         }
     }
     while (i < n_strings) {
-        if (by_tiles(strs[order[i]])) {  // done by the tiled passes
+        if (by_tile[order[i]]) {  // done by the tiled passes
             i++;
             continue;
         }

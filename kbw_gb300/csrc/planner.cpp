@@ -179,4 +179,58 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
     return out;
 }
 
+uint32_t PauliPass::local(uint64_t mask) const {
+    uint32_t r = (uint32_t)(mask & ((1ull << l) - 1));
+    for (uint32_t j = 0; j < m; j++)
+        if (mask >> hq[j] & 1) r |= 1u << (l + j);
+    return r;
+}
+
+// Largest contiguous low block l >= 5 such that l plus the bits of `need`
+// above it fit K; -1 if none.
+static int pauli_low_bits(uint64_t need, int K) {
+    for (int l = K; l >= kLaneBits; l--) {
+        const uint64_t above = need & ~((1ull << l) - 1);
+        if (l + __builtin_popcountll(above) <= K) return l;
+    }
+    return -1;
+}
+
+std::vector<PauliPass> plan_pauli_passes(uint32_t n, int K, const std::vector<uint64_t> &xmasks, size_t max_terms,
+                                         std::vector<size_t> &wide) {
+    std::vector<PauliPass> out;
+    std::vector<size_t> pend;
+    wide.clear();
+    for (size_t k = 0; k < xmasks.size(); k++) {
+        if (pauli_low_bits(xmasks[k], K) >= 0)
+            pend.push_back(k);
+        else
+            wide.push_back(k);
+    }
+    while (!pend.empty()) {
+        uint64_t needed = 0;
+        std::vector<size_t> take, rest;
+        for (size_t k : pend) {
+            const uint64_t nn = needed | xmasks[k];
+            if (take.size() < max_terms && pauli_low_bits(nn, K) >= 0) {
+                needed = nn;
+                take.push_back(k);
+            } else {
+                rest.push_back(k);
+            }
+        }
+        PauliPass p;
+        p.l = (uint32_t)pauli_low_bits(needed, K);
+        uint64_t h = needed & ~((1ull << p.l) - 1);
+        for (uint32_t q = p.l; q < n && p.l + __builtin_popcountll(h) < (uint32_t)K; q++) h |= 1ull << q;
+        for (uint32_t q = 0; q < 64; q++)
+            if (h >> q & 1) p.hq[p.m++] = (uint8_t)q;
+        p.tile_mask = ((1ull << p.l) - 1) | h;
+        p.members = std::move(take);
+        out.push_back(std::move(p));
+        pend.swap(rest);
+    }
+    return out;
+}
+
 }  // namespace kbwg

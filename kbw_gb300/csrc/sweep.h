@@ -123,4 +123,18 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
 
 bool is_diagonal(uint32_t kind);
 
+// Passes over tiles of 2^K amplitudes for Pauli strings: a pass holds the
+// strings whose flip mask fits one tile (local bits 0..l-1 = qubits 0..l-1,
+// l..l+m-1 = qubits hq[]), at most max_terms of them.  Strings with flip
+// masks too wide for any tile are returned in `wide`.
+struct PauliPass {
+    uint32_t l = 0, m = 0;
+    uint8_t hq[16] = {0};
+    uint64_t tile_mask = 0;           // global qubits held by the tile
+    std::vector<size_t> members;      // indices into the input masks
+    uint32_t local(uint64_t mask) const;  // qubit mask -> local bit mask (qubits in the tile)
+};
+std::vector<PauliPass> plan_pauli_passes(uint32_t n, int K, const std::vector<uint64_t> &xmasks, size_t max_terms,
+                                         std::vector<size_t> &wide);
+
 }  // namespace kbwg
