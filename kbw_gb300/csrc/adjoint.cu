@@ -340,7 +340,7 @@ struct AdjKernel {
 };
 
 template <class P, int K, int R>
-__global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads)
+__global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     k_adjoint(typename P::Mem *__restrict__ phi, typename P::Mem *__restrict__ lam, const __grid_constant__ AdjParams a) {
     using Amp = typename P::Amp;
     using Mem = typename P::Mem;
