@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/kbwg.h"
@@ -199,9 +200,20 @@ struct Grad<Fast<T>> {
         }
     }
     static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
-    static __device__ __forceinline__ double warp_total(Acc a) {
+    static __device__ __forceinline__ Acc warp_sum(Acc a) {
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        return (double)a;
+        return a;
+    }
+    // per-warp accumulator across tiles: float-float for complex64 (no FP64
+    // instruction in the sweep), binary64 for complex128
+    using Wacc = typename std::conditional<sizeof(T) == 4, ff::f2, double>::type;
+    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) {
+        if constexpr (sizeof(T) == 4) return ff::add(w, ff::f2{a, 0.f});
+        else return w + a;
+    }
+    static __device__ __forceinline__ double wvalue(Wacc w) {
+        if constexpr (sizeof(T) == 4) return (double)w.h + (double)w.l;
+        else return w;
     }
 };
 
@@ -235,13 +247,16 @@ struct Grad<FFPol> {
         }
     }
     static __device__ __forceinline__ Acc add(Acc a, Acc b) { return ff::add(a, b); }
-    static __device__ __forceinline__ double warp_total(Acc a) {
+    static __device__ __forceinline__ Acc warp_sum(Acc a) {
         for (int o = 16; o > 0; o >>= 1) {
             Acc b{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
             a = ff::add(a, b);
         }
-        return (double)a.h + (double)a.l;
+        return a;
     }
+    using Wacc = ff::f2;
+    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return ff::add(w, a); }
+    static __device__ __forceinline__ double wvalue(Wacc w) { return (double)w.h + (double)w.l; }
 };
 
 template <class P, int R, int B>
@@ -360,8 +375,10 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     q += kMaxSweepGates * sizeof(TileGate);
     uint32_t *sinfo = reinterpret_cast<uint32_t *>(q);
     q += kMaxSweepGates * sizeof(uint32_t);
-    double *acc = reinterpret_cast<double *>(q);  // [kWarps][kMaxSweepGates]
-    q += (size_t)AK::kWarps * kMaxSweepGates * sizeof(double);
+    using Wacc = typename G::Wacc;
+    static_assert(sizeof(Wacc) == sizeof(double), "per-warp accumulator slot");
+    Wacc *acc = reinterpret_cast<Wacc *>(q);  // [kWarps][kMaxSweepGates]
+    q += (size_t)AK::kWarps * kMaxSweepGates * sizeof(Wacc);
     uint64_t *bar = reinterpret_cast<uint64_t *>(q);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -374,7 +391,7 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
         sg[i] = p.prog[i];
         sinfo[i] = a.ginfo[i];
     }
-    for (uint32_t i = threadIdx.x; i < (uint32_t)AK::kWarps * kMaxSweepGates; i += blockDim.x) acc[i] = 0.0;
+    for (uint32_t i = threadIdx.x; i < (uint32_t)AK::kWarps * kMaxSweepGates; i += blockDim.x) acc[i] = Wacc{};
     for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
         uint64_t off = 0;
         for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
@@ -454,8 +471,11 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
                 const uint32_t info = sinfo[gi];
                 const int gt = (int)(info & 15u);
                 if (gt != GT_NONE) {
-                    const double w = G::warp_total(grad_partial<P, K, R>(g, gt, vp, vl, R0, F, base));
-                    if (lane == 0) acc[warp * kMaxSweepGates + (info >> 4)] += w;
+                    const typename G::Acc w = G::warp_sum(grad_partial<P, K, R>(g, gt, vp, vl, R0, F, base));
+                    if (lane == 0) {
+                        Wacc &slot = acc[warp * kMaxSweepGates + (info >> 4)];
+                        slot = G::wadd(slot, w);
+                    }
                 }
                 tile_gate<P, K, R>(g, vp, R0, F, base);
                 tile_gate<P, K, R>(g, vl, R0, F, base);
@@ -477,7 +497,7 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     __syncthreads();
     for (uint32_t sl = threadIdx.x; sl < a.nslots; sl += blockDim.x) {
         double t = 0.0;
-        for (int w = 0; w < AK::kWarps; w++) t += acc[w * kMaxSweepGates + sl];
+        for (int w = 0; w < AK::kWarps; w++) t += G::wvalue(acc[w * kMaxSweepGates + sl]);
         a.partials[(size_t)blockIdx.x * a.nslots + sl] = t;
     }
 }
