@@ -11,6 +11,27 @@ bool is_diagonal(uint32_t kind) { return is_diag_kind(kind); }
 
 static inline uint64_t qubits_of(const GateDesc &g) { return g.ctrl | (1ull << g.target); }
 
+// Gates left behind (deferred), summarised for commutation: `any` = every
+// qubit they touch, `ndt` = the targets of their non-diagonal gates.  Two
+// gates commute when every qubit they share is acted on diagonally by both
+// (a control, or a diagonal gate's qubit), so a later gate may pass the
+// deferred ones iff it touches no deferred non-diagonal target and, if it is
+// non-diagonal, its own target is untouched by them.
+struct Deferred {
+    uint64_t any = 0, ndt = 0;
+    bool all = false;  // order-preserving mode: nothing passes
+    bool passes(const GateDesc &x) const {
+        if (all) return false;
+        if (qubits_of(x) & ndt) return false;
+        return is_diagonal(x.kind) || !((any >> x.target) & 1);
+    }
+    void add(const GateDesc &x, bool keep_order) {
+        any |= qubits_of(x);
+        if (!is_diagonal(x.kind)) ndt |= 1ull << x.target;
+        if (keep_order) all = true;
+    }
+};
+
 // Choose the tile's contiguous low block l (as large as possible) and its
 // high qubits: every needed high target, padded up to K qubits.
 static void choose_tile(uint32_t n, int K, uint64_t needed, PlannedSweep &sw) {
@@ -47,35 +68,56 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
     std::vector<size_t> remaining(count);
     for (size_t i = 0; i < count; i++) remaining[i] = i;
     const size_t window = 8192;  // gates examined per sweep
-    while (!remaining.empty()) {
-        // 1. choose the sweep's gates
-        uint64_t needed = 0, blocked = 0;
-        const int max_high = K - kLaneBits;
-        std::vector<size_t> take, rest;
+    const int max_high = K - kLaneBits;
+    // Greedy selection of a sweep's gates.  grow: the admissible high targets
+    // (bits >= 5) are collected first come, first served up to max_high;
+    // otherwise they are the fixed set `needed`.
+    auto select = [&](uint64_t needed, bool grow, std::vector<size_t> *take, std::vector<size_t> *rest) {
+        Deferred blocked;
+        size_t taken = 0;
         const size_t scan = std::min(remaining.size(), window);
         for (size_t ii = 0; ii < scan; ii++) {
             const size_t i = remaining[ii];
             const GateDesc &x = g[i];
-            const uint64_t qs = qubits_of(x);
-            bool ok = !(qs & blocked) && take.size() < (size_t)kMaxSweepGates;
+            bool ok = blocked.passes(x) && taken < (size_t)kMaxSweepGates;
             if (ok && !is_diagonal(x.kind) && x.target >= (uint32_t)kLaneBits) {
                 const uint64_t b = 1ull << x.target;
                 if (!(needed & b)) {
-                    if (__builtin_popcountll(needed) < max_high)
+                    if (grow && __builtin_popcountll(needed) < max_high)
                         needed |= b;
                     else
                         ok = false;
                 }
             }
             if (ok) {
-                take.push_back(i);
+                taken++;
+                if (take) take->push_back(i);
             } else {
-                rest.push_back(i);
-                blocked |= qs;
-                if (keep_order) blocked = ~0ull;  // nothing may pass a deferred gate
+                if (rest) rest->push_back(i);
+                blocked.add(x, keep_order);
             }
         }
-        for (size_t ii = scan; ii < remaining.size(); ii++) rest.push_back(remaining[ii]);
+        if (rest)
+            for (size_t ii = scan; ii < remaining.size(); ii++) rest->push_back(remaining[ii]);
+        return std::make_pair(taken, needed);
+    };
+    while (!remaining.empty()) {
+        // 1. choose the sweep's gates: first-come high targets, or the window
+        // of max_high consecutive qubits that admits the most gates
+        auto best = select(0, true, nullptr, nullptr);
+        bool best_grow = true;
+        if (!keep_order && n > (uint32_t)K) {
+            for (uint32_t a = kLaneBits; a + max_high <= n; a++) {
+                const uint64_t w = ((1ull << max_high) - 1) << a;
+                const auto c = select(w, false, nullptr, nullptr);
+                if (c.first > best.first) {
+                    best = c;
+                    best_grow = false;
+                }
+            }
+        }
+        std::vector<size_t> take, rest;
+        const uint64_t needed = select(best_grow ? 0 : best.second, best_grow, &take, &rest).second;
 
         PlannedSweep sw;
         choose_tile(n, K, needed, sw);
@@ -101,18 +143,16 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                 break;
             }
             std::vector<size_t> now, later;
-            uint64_t blk = 0;
+            Deferred blk;
             for (size_t i : pending) {
                 const GateDesc &x = g[i];
-                const uint64_t qs = qubits_of(x);
-                bool ok = !(qs & blk);
+                bool ok = blk.passes(x);
                 if (ok && !is_diagonal(x.kind)) ok = runs_in(local_bit(sw, x.target), layout, K, R);
                 if (ok) {
                     now.push_back(i);
                 } else {
                     later.push_back(i);
-                    blk |= qs;
-                    if (keep_order) blk = ~0ull;
+                    blk.add(x, keep_order);
                 }
             }
             if (now.empty()) {
