@@ -222,8 +222,9 @@ int32_t kbwg_build_info(const uint8_t **msg, uintptr_t *size);
  * report how the engine would execute it: order[] receives the gate indices
  * in execution order, sweep_end[k] the end (exclusive) in order[] of sweep k,
  * tile_mask[k] the qubits of sweep k's tile.  The arrays need n_gates
- * entries.  With precision KBWG_C64 tiles have 13 qubits, with KBWG_C128 12;
- * num_qubits must be at least that.  flags: KBWG_FLAG_EXACT_ORDER or 0. */
+ * entries.  With precision KBWG_C64 tiles have 13 qubits, with KBWG_C128 12
+ * (11 with KBWG_FLAG_FAST_C128); num_qubits must be at least that.  flags:
+ * KBWG_FLAG_EXACT_ORDER, KBWG_FLAG_FAST_C128 or 0. */
 int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
                   uintptr_t n_gates, uint32_t *order, uint32_t *sweep_end, uint64_t *tile_mask,
                   uintptr_t *n_sweeps);

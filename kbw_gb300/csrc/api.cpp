@@ -890,8 +890,9 @@ int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const
     GUARD_BEGIN
     if (!n_sweeps || (n_gates && (!gates || !order || !sweep_end || !tile_mask)))
         return fail(KBWG_EINVAL, "null argument");
-    const int K = precision ? TileCfg<double>::K : TileCfg<float>::K;
-    const int R = precision ? TileCfg<double>::R : TileCfg<float>::R;
+    const bool ff = precision && (flags & KBWG_FLAG_FAST_C128);
+    const int K = ff ? TileCfgFF::K : precision ? TileCfg<double>::K : TileCfg<float>::K;
+    const int R = ff ? TileCfgFF::R : precision ? TileCfg<double>::R : TileCfg<float>::R;
     if (num_qubits < (uintptr_t)K || num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits outside [K, 32]");
     std::vector<GateDesc> gd(n_gates);
     for (uintptr_t i = 0; i < n_gates; i++) {

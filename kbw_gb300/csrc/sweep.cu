@@ -43,10 +43,11 @@ struct SweepKernel {
     static constexpr size_t kTileBytes = sizeof(Mem) << K;
     static constexpr size_t kChunkTable = 256 * sizeof(uint64_t);
     static constexpr size_t kSmem = kTileBytes + kChunkTable + kMaxSweepGates * sizeof(TileGate) + 16;
+    static constexpr int kCtasPerSm = (R == 3) ? 3 : 2;  // register budget: 80 resp. 128 (c128) / 64 (c64)
 };
 
 template <class P, int K, int R>
-__global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, 2)
+__global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P, K, R>::kCtasPerSm)
     k_sweep(typename P::Mem *__restrict__ st, const __grid_constant__ SweepParams p) {
     using Amp = typename P::Amp;
     using Mem = typename P::Mem;
@@ -289,7 +290,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     }
     const TileGate *dprog = (const TileGate *)dbuf;
     const uint64_t tiles = 1ull << (s.n - K);
-    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * 2);
+    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * SK::kCtasPerSm);
     if (graphs) {
         e = cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) {
@@ -448,7 +449,7 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
 }
 
 bool ff_capable(const Sim &s) {
-    return s.prec && (s.flags & KBWG_FLAG_FAST_C128) && s.n >= (uint32_t)TileCfg<double>::K;
+    return s.prec && (s.flags & KBWG_FLAG_FAST_C128) && s.n >= (uint32_t)TileCfgFF::K;
 }
 
 cudaError_t ensure_binary64(Sim &s) {
@@ -476,7 +477,7 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
             s.ff_resident = true;
         }
         std::vector<GateDesc> g = ff_rewrite(gates, count);
-        return run_fused_p<FF2, TileCfg<double>::K, TileCfg<double>::R>(s, g.data(), g.size());
+        return run_fused_p<FF2, TileCfgFF::K, TileCfgFF::R>(s, g.data(), g.size());
     }
     return s.prec ? run_fused_t<double>(s, gates, count) : run_fused_t<float>(s, gates, count);
 }

