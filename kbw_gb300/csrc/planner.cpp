@@ -214,7 +214,8 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
         next.reserve(leftover.size() + rest.size());
         std::merge(leftover.begin(), leftover.end(), rest.begin(), rest.end(), std::back_inserter(next));
         remaining.swap(next);
-        if (!sw.gates.empty()) out.push_back(std::move(sw));
+        if (sw.gates.empty()) break;  // no gate placeable (invalid tile geometry): the caller sees the shortfall
+        out.push_back(std::move(sw));
     }
     return out;
 }

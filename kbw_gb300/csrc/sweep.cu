@@ -44,6 +44,9 @@ struct SweepKernel {
     static constexpr size_t kChunkTable = 256 * sizeof(uint64_t);
     static constexpr size_t kSmem = kTileBytes + kChunkTable + kMaxSweepGates * sizeof(TileGate) + 16;
     static constexpr int kCtasPerSm = (R == 3) ? 3 : 2;  // register budget: 80 resp. 128 (c128) / 64 (c64)
+    // register layouts A = bits [5, 5+R) and B = [K-R, K) must cover every
+    // local bit above the lanes, or a gate on the gap could never run
+    static_assert(K <= kLaneBits + 2 * R, "tile geometry leaves local bits no layout holds in registers");
 };
 
 template <class P, int K, int R>
@@ -273,6 +276,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         src.insert(src.end(), sw.src.begin(), sw.src.end());
     }
     const size_t total = planned.size();
+    if (total != count) return cudaErrorInvalidValue;  // the planner could not place every gate
     void *dbuf = nullptr;
     cudaError_t e;
     if (graphs) {
