@@ -3,7 +3,8 @@
 // A tile is 2^K amplitudes: its local bits 0..l-1 are the global qubits
 // 0..l-1 (a contiguous chunk of 2^l amplitudes) and its local bits l..K-1 are
 // m = K-l arbitrary higher qubits, so a tile is 2^m chunks.  Persistent CTAs
-// (two per SM) walk the tiles; per CTA:
+// (two or three per SM, by the register budget of the geometry) walk the
+// tiles; per CTA:
 //   * once per launch the sweep's gate program and the chunk-offset table are
 //     staged in shared memory;
 //   * per tile, warp 0 issues one TMA bulk copy (cp.async.bulk ... mbarrier::
