@@ -83,12 +83,14 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
     }
     __syncthreads();
 
-    auto tile_base = [&](uint64_t tau) {
-        uint64_t b = tau << l;
+    // state indices fit 32 bits (at most 32 qubits): 32-bit tile indices keep
+    // registers free for the amplitudes
+    auto tile_base = [&](uint32_t tau) {
+        uint32_t b = tau << l;
         for (uint32_t j = 0; j < m; j++) b = insert_zero_at(b, p.hq[j]);
         return b;
     };
-    auto issue_load = [&](uint64_t tau) {
+    auto issue_load = [&](uint32_t tau) {
         if (warp == 0) {
             const uint64_t b = tile_base(tau);
             if (lane == 0) mbar_expect_tx(bar, (uint32_t)SK::kTileBytes);
@@ -98,12 +100,12 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
         }
     };
 
-    uint64_t tau = blockIdx.x;
+    uint32_t tau = blockIdx.x;
     if (tau < p.tiles) issue_load(tau);
     const uint32_t FA = (uint32_t)lane | ((uint32_t)warp << (kLaneBits + R));
     const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
     for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
-        const uint64_t base = tile_base(tau);
+        const uint32_t base = tile_base(tau);
         bool ok = false;
         for (uint32_t spin = 0; spin < (1u << 22); spin++)
             if (mbar_try_wait(bar, it & 1u)) {
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
         // the tile buffer is free: start the next tile's load, then store this one
         fence_proxy_async();
         __syncthreads();
-        const uint64_t next = tau + gridDim.x;
+        const uint32_t next = tau + gridDim.x;
         if (next < p.tiles) issue_load(next);
 #pragma unroll
         for (int j = 0; j < NR; j++) {

@@ -554,12 +554,14 @@ __device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], const T
 // index of local 0.  A few header loads and one jump table per gate.
 template <class P, int K, int R>
 __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int /*R0*/, uint32_t F,
-                                          uint64_t base) {
+                                          uint32_t base) {
     static_assert(R >= 3 && R <= 4, "dispatch covers register bits 0..3");
     const uint32_t op = g.op;
     const uint32_t fneed = g.fneed;
     const uint32_t jm = g.jm;
-    if ((base & g.co) != g.co) return;  // a control outside the tile is 0 for the whole tile
+    // (state indices and control masks fit 32 bits: at most 32 qubits)
+    const uint32_t co = (uint32_t)g.co;
+    if ((base & co) != co) return;  // a control outside the tile is 0 for the whole tile
     const bool fok = (F & fneed) == fneed;
     if (op < OP_REG) {  // lane targets: every lane shuffles, outside the jump table
         if (op == OP_LANE + TG_X) lane_gate<P, R, TG_X>(v, g, fok, F);
@@ -584,7 +586,7 @@ __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v
 #define KBWG_DFIX(C)                                                                                          \
     case OP_DFIX + (C - TG_Z): {                                                                           \
         const uint32_t tb = g.tb, tout = g.tout;                                    \
-        const bool one = (C == TG_SCALE) || (tb == TG_OUTER ? ((base >> tout) & 1ull) != 0 : ((F >> tb) & 1u) != 0); \
+        const bool one = (C == TG_SCALE) || (tb == TG_OUTER ? ((base >> tout) & 1u) != 0 : ((F >> tb) & 1u) != 0); \
         diag_fixed<P, R, C>(v, g, jm, one);                                                                 \
         break;                                                                                              \
     }
