@@ -220,6 +220,45 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
     return out;
 }
 
+// ---- diagonal folding -------------------------------------------------------------
+static void diag_sides(const GateDesc &x, double s[4]) {  // |0> and |1> phases (re, im)
+    s[0] = 1.0, s[1] = 0.0, s[2] = 1.0, s[3] = 0.0;
+    if (x.kind == G_Z) s[2] = -1.0;
+    else if (x.kind == G_P) s[2] = x.c[0], s[3] = x.c[1];
+    else s[0] = x.c[0], s[1] = x.c[1], s[2] = x.c[2], s[3] = x.c[3];  // G_RZ slot convention
+}
+
+std::vector<GateDesc> fold_diagonals(const GateDesc *g, size_t count) {
+    std::vector<GateDesc> out;
+    out.reserve(count);
+    int64_t pend[64];
+    for (int q = 0; q < 64; q++) pend[q] = -1;
+    for (size_t i = 0; i < count; i++) {
+        const GateDesc &x = g[i];
+        const bool fold = x.ctrl == 0 && (x.kind == G_Z || x.kind == G_P || x.kind == G_RZ);
+        if (fold && pend[x.target] >= 0) {
+            GateDesc &y = out[(size_t)pend[x.target]];
+            double a[4], b[4];
+            diag_sides(y, a);
+            diag_sides(x, b);
+            const double s0r = a[0] * b[0] - a[1] * b[1], s0i = a[0] * b[1] + a[1] * b[0];
+            const double s1r = a[2] * b[2] - a[3] * b[3], s1i = a[2] * b[3] + a[3] * b[2];
+            if (s0r == 1.0 && s0i == 0.0) {  // |0> untouched: a phase gate
+                y.kind = G_P;
+                y.c[0] = s1r, y.c[1] = s1i, y.c[2] = y.c[3] = 0.0;
+            } else {
+                y.kind = G_RZ;
+                y.c[0] = s0r, y.c[1] = s0i, y.c[2] = s1r, y.c[3] = s1i;
+            }
+            continue;
+        }
+        if (!is_diag_kind(x.kind)) pend[x.target] = -1;  // a non-diagonal action on its target
+        out.push_back(x);
+        if (fold) pend[x.target] = (int64_t)out.size() - 1;
+    }
+    return out;
+}
+
 uint32_t PauliPass::local(uint64_t mask) const {
     uint32_t r = (uint32_t)(mask & ((1ull << l) - 1));
     for (uint32_t j = 0; j < m; j++)

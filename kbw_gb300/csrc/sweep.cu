@@ -427,8 +427,9 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
                 continue;
             }
         } else if (x.kind == G_RZ && x.ctrl == 0) {
-            // e^{-it/2} diag(1, e^{it}): e^{it} = (c2 + i c3)^2
-            const double c = x.c[2] * x.c[2] - x.c[3] * x.c[3], sn = 2.0 * x.c[2] * x.c[3];
+            // diag(u0, u1) = u0 diag(1, u1 conj(u0)) for unit u0 (for RZ(t):
+            // u1 conj(u0) = e^{it}; also a folded general diagonal)
+            const double c = x.c[2] * x.c[0] + x.c[3] * x.c[1], sn = x.c[3] * x.c[0] - x.c[2] * x.c[1];
             const double nr = gr * x.c[0] - gi * x.c[1], ni = gr * x.c[1] + gi * x.c[0];
             gr = nr;
             gi = ni;
@@ -475,6 +476,12 @@ cudaError_t init_state(Sim &s) {
 }
 
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
+    std::vector<GateDesc> folded;
+    if (!(s.flags & KBWG_FLAG_EXACT_ORDER)) {
+        folded = fold_diagonals(gates, count);
+        gates = folded.data();
+        count = folded.size();
+    }
     if (ff_capable(s)) {
         // float-float sweeps read and write the float-float form; the state
         // stays in it until an operation needs binary64

@@ -130,6 +130,14 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
 
 bool is_diagonal(uint32_t kind);
 
+// Fold each uncontrolled diagonal one-qubit gate (Z, P, RZ) into an earlier
+// one on the same qubit when no gate in between acts non-diagonally on that
+// qubit (those gates touch it only as a control or diagonally, so they
+// commute with it).  A merged gate is a phase gate, or a general diagonal in
+// the RZ slots (|0> phase c0 + i c1, |1> phase c2 + i c3).  Changes rounding
+// only; not used when the program order must be kept.
+std::vector<GateDesc> fold_diagonals(const GateDesc *g, size_t count);
+
 // Passes over tiles of 2^K amplitudes for Pauli strings: a pass holds the
 // strings whose flip mask fits one tile (local bits 0..l-1 = qubits 0..l-1,
 // l..l+m-1 = qubits hq[]), at most max_terms of them.  Strings with flip

@@ -452,3 +452,33 @@ def test_graph_replay_same_structure_new_angles(prec, fast):
         ref.apply(circ)
         assert rel_err(a.state(), ref.state()) < tol
         assert rel_err(a.state(), b.state()) < tol
+
+
+@pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", False), ("c128", True)])
+def test_folded_diagonal_chains(prec, fast):
+    """Runs of diagonal gates (Z, S, T, P, RZ) on a qubit separated only by
+    gates that touch it as a control or diagonally are folded into one gate
+    on the host; results match the oracle, which applies every gate."""
+    n = 15
+    rng = np.random.default_rng(301)
+    circ = []
+    for _ in range(400):
+        q = int(rng.integers(0, n))
+        r = rng.random()
+        if r < 0.45:  # diagonal one-qubit
+            kind = [C.Z, C.P, C.RZ][int(rng.integers(0, 3))]
+            circ.append((kind, q, (), float(rng.uniform(0, 2 * math.pi))))
+        elif r < 0.75:  # CNOT with q as control: keeps q's diagonal run open
+            t = int((q + 1 + rng.integers(0, n - 1)) % n)
+            circ.append((C.X, t, (q,), 0.0))
+        elif r < 0.85:  # controlled phase: diagonal on both qubits
+            c = int((q + 1 + rng.integers(0, n - 1)) % n)
+            circ.append((C.P, q, (c,), float(rng.uniform(0, 2 * math.pi))))
+        else:  # non-diagonal on q: closes the run
+            kind = [C.H, C.RX, C.RY, C.Y][int(rng.integers(0, 4))]
+            circ.append((kind, q, (), float(rng.uniform(0, 2 * math.pi))))
+    sim = DenseGB300(n, prec, fast_c128=fast)
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, prec)
+    ref.apply(circ)
+    assert rel_err(sim.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
