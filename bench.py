@@ -417,6 +417,10 @@ def run_batch_bench(args, torch, C):
             "config": "hea-batch n~U{8..20} L~U{2..8} ring-TFIM, one persistent launch (incl. host<->device copies)"}
 
 
+def rounded(d, digits=3):
+    return {k: round(v, digits) if isinstance(v, float) else v for k, v in d.items()}
+
+
 def run_ours(args, world, rank, local):
     import torch
     import kbw_gb300
@@ -437,6 +441,9 @@ def run_ours(args, world, rank, local):
 
     sim = DenseGB300(n, prec, fast_c128=fast)
     ext = torch.cuda.ExternalStream(sim.stream_handle())
+    # tile size and fusion depth picked by the engine's autotuner on this
+    # circuit (before the warm-up; the handle's state is left unchanged)
+    tuning = rounded(sim.autotune(circ, reps=1) if args.tune else sim.tuning())
 
     def step():
         sim.apply(circ)
@@ -539,6 +546,7 @@ def run_ours(args, world, rank, local):
                                       "note": "IEEE binary64 gate arithmetic: FP64-issue bound on GB300"}
         exact.close()
         s64 = DenseGB300(n, "c64")
+        tuning64 = rounded(s64.autotune(circ, reps=1) if args.tune else s64.tuning())
         ms64, nl64, kms64, kb64 = time_steps(s64, circ, args.steps, 2, torch)
         ach64 = kb64 / (kms64 * 1e-3) / 1e9
         sweeps64 = s64.last_flush_stats()[1]
@@ -548,7 +556,7 @@ def run_ours(args, world, rank, local):
                             "dtype": "f32",
                             "roofline": {"achieved": round(ach64, 1), "frac": round(ach64 / peak, 4),
                                          "avg_launch_ms": round(kms64 / max(nl64, 1), 4)},
-                            "single_gate_sweep": single64}
+                            "single_gate_sweep": single64, "tuning": tuning64}
         s64.close()
     else:
         sim.close()
@@ -581,7 +589,7 @@ def run_ours(args, world, rank, local):
                        "layers": args.layers, "gates": G, "precision": prec,
                        "arithmetic": "float-float" if fast else "native", "sweeps_per_step": passes,
                        "l2": "state %d GiB > 129 MB L2; no flush needed" % ((B << n) >> 30),
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
             "sweep_gbs": round(world * passes * 2 * B * (1 << n) / (ms_step * 1e-3) / 1e9, 1),
             "gpu_launches": launches,
             "roofline": roofline, "single_gate_sweep": single, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
@@ -603,6 +611,8 @@ def main():
                     help="complex128 gate arithmetic: float-float (default) or IEEE binary64")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="keep the default tile size and fusion depth instead of autotuning them")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-gates", type=int, default=4)
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")

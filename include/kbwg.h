@@ -254,6 +254,60 @@ int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative);
 /* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
 int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
 
+/* ---- sweep tuning (no counterpart in the reference) ---------------------- */
+
+/* Gate calls run as fused sweeps (one pass over the state applies many
+ * gates).  Two settings shape them: the tile size (2^tile_qubits amplitudes
+ * staged per tile; each arithmetic has a few compiled sizes) and the fusion
+ * depth (the most gates one sweep applies, 1..256).  The environment
+ * variables KBWG_TILE_QUBITS and KBWG_FUSION_DEPTH set them for every handle
+ * kbwg_new creates (kbwg_new fails with KBWG_EINVAL on a value no kernel
+ * exists for); a tile size larger than a handle's qubit count falls back to
+ * the default on that handle.  They apply wherever gates are applied to a
+ * handle's state (gate calls, the forward pass of kbwg_adjoint_gradient, the
+ * circuit runs of kbwg_param_shift_gradient), not to the adjoint's reverse
+ * sweeps or to the batch and reduction kernels. */
+enum {
+    KBWG_TUNE_DEFAULT = 0, /* built-in defaults */
+    KBWG_TUNE_SET = 1,     /* kbwg_set_tuning */
+    KBWG_TUNE_ENV = 2,     /* KBWG_TILE_QUBITS / KBWG_FUSION_DEPTH */
+    KBWG_TUNE_TIMED = 3,   /* kbwg_autotune timed the candidates */
+    KBWG_TUNE_CACHED = 4   /* kbwg_autotune reused this process's earlier result */
+};
+typedef struct kbwg_tuning {
+    uint32_t tile_qubits;      /* tile size the next flush uses; 0 = one kernel per gate */
+    uint32_t fusion_depth;     /* most gates one sweep applies */
+    uint32_t source;           /* KBWG_TUNE_* */
+    uint32_t candidates;       /* (tile size, depth) pairs the last kbwg_autotune timed */
+    double ms_per_run;         /* device time of one run of the tuned circuit, chosen settings */
+    double default_ms_per_run; /* the same with the default settings */
+} kbwg_tuning;
+
+/* Tile sizes with a compiled sweep kernel for this handle's arithmetic and
+ * qubit count, the default first (none when the handle runs one kernel per
+ * gate).  capacity >= 4 always suffices. */
+int32_t kbwg_tile_options(kbwg_sim *sim, uint32_t *tile_qubits, uintptr_t capacity, uintptr_t *n);
+
+/* Set the tile size (0 = default, else one of kbwg_tile_options) and the
+ * fusion depth (0 = default 256, else 1..256); KBWG_EINVAL otherwise.
+ * Applies from the next flush; queued gates stay queued. */
+int32_t kbwg_set_tuning(kbwg_sim *sim, uint32_t tile_qubits, uint32_t fusion_depth);
+int32_t kbwg_get_tuning(kbwg_sim *sim, kbwg_tuning *out);
+
+/* Autotuner: runs the circuit (gates, as for kbwg_apply_gates) under every
+ * compiled tile size x fusion depths {256, 64, 16}, each 2 + reps times
+ * (reps 0 = 1), times the last reps with CUDA events on the handle's
+ * stream, and sets the fastest pair on the handle.  Queued gates are flushed
+ * first; the state is copied aside and put back afterwards, so the handle's
+ * state is unchanged (this needs device memory for one more state:
+ * KBWG_ENOMEM otherwise, settings unchanged).  Results are cached for the
+ * process by device, qubit count, arithmetic and circuit structure (kinds,
+ * targets, controls; not angles): a later call with the same structure
+ * times nothing.  With KBWG_TILE_QUBITS or KBWG_FUSION_DEPTH in the
+ * environment the override stands and nothing is timed.  out may be NULL. */
+int32_t kbwg_autotune(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates, uint32_t reps,
+                      kbwg_tuning *out);
+
 /* ---- allocation-free entry (no counterpart in the reference) ------------- */
 
 /* For callers that cannot allocate device memory: code recorded into a CUDA

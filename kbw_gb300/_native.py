@@ -29,6 +29,14 @@ class Gate(ctypes.Structure):
                 ("control_mask", ctypes.c_uint64), ("angle", ctypes.c_double)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("tile_qubits", ctypes.c_uint32), ("fusion_depth", ctypes.c_uint32),
+                ("source", ctypes.c_uint32), ("candidates", ctypes.c_uint32),
+                ("ms_per_run", ctypes.c_double), ("default_ms_per_run", ctypes.c_double)]
+
+
+TUNE_SOURCES = ("default", "set", "env", "timed", "cached")
+
 # name -> (restype, argtypes); every function declared in include/kbwg.h
 _P = ctypes.c_void_p
 _U = ctypes.c_size_t  # uintptr_t
@@ -77,6 +85,10 @@ SIGNATURES = {
     "kbwg_profile_read": (_I32, [_P, _U64P, _DP, _DP]),
     "kbwg_transfer_bytes": (_I32, [_U64P, _U64P]),
     "kbwg_state_distance": (_I32, [_P, _P, _DP]),
+    "kbwg_tile_options": (_I32, [_P, ctypes.POINTER(ctypes.c_uint32), _U, _UP]),
+    "kbwg_set_tuning": (_I32, [_P, ctypes.c_uint32, ctypes.c_uint32]),
+    "kbwg_get_tuning": (_I32, [_P, ctypes.c_void_p]),
+    "kbwg_autotune": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.c_uint32, ctypes.c_void_p]),
     "kbwg_masked_norm_noalloc": (_I32, [_P, _U, _I32, ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "kbwg_last_error": (ctypes.c_char_p, []),
     "kbwg_launch_count": (ctypes.c_uint64, []),

@@ -15,6 +15,7 @@
 #include "../../include/kbwg.h"
 #include "sim.h"
 #include "sweep.h"
+#include "tune.h"
 
 namespace kbwg {
 
@@ -178,6 +179,43 @@ static int32_t select_device(kbwg_sim *s) {
         if (_r) return _r;                                    \
     }
 
+// KBWG_TILE_QUBITS / KBWG_FUSION_DEPTH: sweep settings for every new handle.
+static bool env_u32(const char *name, uint32_t &v, bool &present) {
+    const char *t = getenv(name);
+    present = t && *t;
+    if (!present) return true;
+    char *end = nullptr;
+    const unsigned long x = strtoul(t, &end, 10);
+    if (!end || *end || x > 0xFFFFFFFFul) return false;
+    v = (uint32_t)x;
+    return true;
+}
+
+static bool env_tuning_set() {
+    const char *a = getenv("KBWG_TILE_QUBITS"), *b = getenv("KBWG_FUSION_DEPTH");
+    return (a && *a) || (b && *b);
+}
+
+static int32_t apply_env_tuning(Sim &s, std::string &msg) {
+    uint32_t k = 0, d = 0;
+    bool hk = false, hd = false;
+    if (!env_u32("KBWG_TILE_QUBITS", k, hk)) return msg = "KBWG_TILE_QUBITS is not a number", KBWG_EINVAL;
+    if (!env_u32("KBWG_FUSION_DEPTH", d, hd)) return msg = "KBWG_FUSION_DEPTH is not a number", KBWG_EINVAL;
+    if (hk) {
+        const std::vector<uint32_t> ks = compiled_tiles(s);
+        if (k && std::find(ks.begin(), ks.end(), k) == ks.end())
+            return msg = "KBWG_TILE_QUBITS=" + std::to_string(k) + ": no sweep kernel of that tile size for this arithmetic",
+                   KBWG_EINVAL;
+        s.tile_k = k;
+    }
+    if (hd) {
+        if (d > (uint32_t)kMaxSweepGates) return msg = "KBWG_FUSION_DEPTH must be 0..256", KBWG_EINVAL;
+        s.fusion_depth = d;
+    }
+    if (hk || hd) s.tune_source = KBWG_TUNE_ENV;
+    return KBWG_OK;
+}
+
 template <class F>
 static auto dispatch(kbwg_sim *s, F &&f) -> decltype(f((float *)nullptr)) {
     return s->prec ? f((double *)nullptr) : f((float *)nullptr);
@@ -229,6 +267,9 @@ int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_s
     char *end = nullptr;
     unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
     s->rng = (seed && end && *end == 0 && *seed) ? (uint64_t)sv : (uint64_t)(uintptr_t)s ^ 0x5DEECE66Dull;
+    std::string tmsg;
+    const int32_t trc = apply_env_tuning(*s, tmsg);
+    if (trc != KBWG_OK) return cleanup(trc, tmsg);
     e = init_state(*s);
     if (e != cudaSuccess) return cleanup(KBWG_ECUDA, cudaGetErrorString(e));
     e = cudaStreamSynchronize(s->stream);
@@ -987,6 +1028,80 @@ int32_t kbwg_last_flush_stats(kbwg_sim *s, uint64_t *gates, uint64_t *passes) {
     if (gates) *gates = s->last_gates;
     if (passes) *passes = s->last_passes;
     return KBWG_OK;
+}
+
+static void fill_tuning(const Sim &s, kbwg_tuning *out) {
+    out->tile_qubits = effective_tile_k(s);
+    out->fusion_depth = s.fusion_depth ? s.fusion_depth : (uint32_t)kMaxSweepGates;
+    out->source = s.tune_source;
+    out->candidates = s.tune_candidates;
+    out->ms_per_run = s.tune_ms;
+    out->default_ms_per_run = s.tune_default_ms;
+}
+
+int32_t kbwg_tile_options(kbwg_sim *s, uint32_t *tile_qubits, uintptr_t capacity, uintptr_t *n) {
+    GUARD_BEGIN
+    if (!s || !n) return fail(KBWG_EINVAL, "null argument");
+    const std::vector<uint32_t> ks = tile_options(*s);
+    *n = ks.size();
+    if (capacity < ks.size()) return fail(KBWG_ECAPACITY, "tile option buffer too small");
+    if (!ks.empty() && !tile_qubits) return fail(KBWG_EINVAL, "null argument");
+    for (size_t i = 0; i < ks.size(); i++) tile_qubits[i] = ks[i];
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_set_tuning(kbwg_sim *s, uint32_t tile_qubits, uint32_t fusion_depth) {
+    GUARD_BEGIN
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    if (tile_qubits) {
+        const std::vector<uint32_t> ks = tile_options(*s);
+        if (std::find(ks.begin(), ks.end(), tile_qubits) == ks.end())
+            return fail(KBWG_EINVAL, "no sweep kernel of that tile size for this handle");
+    }
+    if (fusion_depth > (uint32_t)kMaxSweepGates) return fail(KBWG_EINVAL, "fusion depth must be 0..256");
+    s->tile_k = tile_qubits;
+    s->fusion_depth = fusion_depth;
+    s->tune_source = (tile_qubits || fusion_depth) ? KBWG_TUNE_SET : KBWG_TUNE_DEFAULT;
+    s->tune_candidates = 0;
+    s->tune_ms = s->tune_default_ms = 0.0;
+    return KBWG_OK;
+    GUARD_END
+}
+
+int32_t kbwg_get_tuning(kbwg_sim *s, kbwg_tuning *out) {
+    if (!s || !out) return fail(KBWG_EINVAL, "null argument");
+    fill_tuning(*s, out);
+    return KBWG_OK;
+}
+
+int32_t kbwg_autotune(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates, uint32_t reps, kbwg_tuning *out) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (n_gates && !gates) return fail(KBWG_EINVAL, "null gate list");
+    const uint64_t all = (s->n >= 64) ? ~0ull : ((1ull << s->n) - 1);
+    std::vector<GateDesc> gd(n_gates);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ || g.target >= s->n || (g.control_mask & ~all) || (g.control_mask & (1ull << g.target)))
+            return fail(KBWG_EINVAL, "bad gate");
+        gd[i] = make_gate_desc(s->prec, g.kind, g.target, g.control_mask, g.angle);
+    }
+    if (!env_tuning_set()) {
+        TuneResult r;
+        std::string msg;
+        const int32_t rc = autotune(*s, gd, reps, r, msg);
+        if (rc != KBWG_OK) return fail(rc, msg.c_str());
+        if (r.candidates || r.cached) {
+            s->tune_source = r.cached ? KBWG_TUNE_CACHED : KBWG_TUNE_TIMED;
+            s->tune_candidates = r.candidates;
+            s->tune_ms = r.ms;
+            s->tune_default_ms = r.default_ms;
+        }
+    }
+    if (out) fill_tuning(*s, out);
+    return KBWG_OK;
+    GUARD_END
 }
 
 const char *kbwg_last_error(void) { return g_last_error.c_str(); }

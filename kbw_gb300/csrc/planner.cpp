@@ -63,7 +63,8 @@ static inline bool runs_in(int lb, int layout, int K, int R) {
 }
 
 std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *g, size_t count,
-                                      bool keep_order) {
+                                      bool keep_order, size_t max_gates) {
+    max_gates = std::min(std::max<size_t>(max_gates, 1), (size_t)kMaxSweepGates);
     std::vector<PlannedSweep> out;
     std::vector<size_t> remaining(count);
     for (size_t i = 0; i < count; i++) remaining[i] = i;
@@ -79,7 +80,7 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
         for (size_t ii = 0; ii < scan; ii++) {
             const size_t i = remaining[ii];
             const GateDesc &x = g[i];
-            bool ok = blocked.passes(x) && taken < (size_t)kMaxSweepGates;
+            bool ok = blocked.passes(x) && taken < max_gates;
             if (ok && !is_diagonal(x.kind) && x.target >= (uint32_t)kLaneBits) {
                 const uint64_t b = 1ull << x.target;
                 if (!(needed & b)) {

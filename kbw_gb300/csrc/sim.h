@@ -70,6 +70,14 @@ struct Sim {
     Profiler prof;
     void *graphs = nullptr;  // replay cache of planned sweeps (sweep.cu)
 
+    // execution settings of the fused sweeps (0 = built-in default): tile
+    // geometry 2^tile_k amplitudes, at most fusion_depth gates per sweep
+    uint32_t tile_k = 0;
+    uint32_t fusion_depth = 0;
+    // where they came from (KBWG_TUNE_*) and the last tuner's measurements
+    uint32_t tune_source = 0, tune_candidates = 0;
+    double tune_ms = 0.0, tune_default_ms = 0.0;
+
     // statistics of the last flush
     uint64_t last_passes = 0;
     uint64_t last_gates = 0;
@@ -94,6 +102,17 @@ cudaError_t flush_queue(Sim &s);
 
 // Fusion planner entry used by flush_queue (sweep.cu).
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
+
+// Tile sizes K (2^K amplitudes per tile) with a compiled sweep kernel for
+// the handle's arithmetic and qubit count, the default first; empty when the
+// handle runs one kernel per gate.  Fusion depths the tuner tries.
+std::vector<uint32_t> tile_options(const Sim &s);
+// The same without the qubit-count filter.
+std::vector<uint32_t> compiled_tiles(const Sim &s);
+uint32_t default_tile_k(const Sim &s);
+// Tile size the next flush uses (0: one kernel per gate).
+uint32_t effective_tile_k(const Sim &s);
+constexpr uint32_t kFusionDepths[] = {256, 64, 16};
 
 double next_draw(Sim &s);
 

@@ -242,6 +242,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         attr_set = true;
     }
     const void *kid = (const void *)k_sweep<P, K, R>;
+    const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
     // timed profiling marks every launch with events, which a graph replay cannot
     bool graphs = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
     std::vector<uint64_t> sig;
@@ -250,6 +251,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         GraphCache &gc = *(GraphCache *)s.graphs;
         sig = structure_of(gates, count);
         sig.push_back((uint64_t)(uintptr_t)kid);
+        sig.push_back(depth);
         const uint64_t h = hash_of(sig);
         bool again = false;
         for (uint64_t x : gc.seen) again = again || x == h;
@@ -271,7 +273,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         }
     }
     std::vector<PlannedSweep> plan =
-        plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0);
+        plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0, depth);
     std::vector<TileGate> planned;
     std::vector<uint32_t> src;
     for (const PlannedSweep &sw : plan) {
@@ -371,9 +373,54 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     return cudaSuccess;
 }
 
+// Tile sizes with a compiled sweep kernel, per arithmetic, default first:
+// complex64 13 (16 amplitudes per thread, 512 threads), 12 (16, 256) and 11
+// (8, 256); binary64 complex128 12 (16) and 11 (8); float-float complex128
+// 11 (8) and 12 (16).  The order-preserving mode has the default only.
+std::vector<uint32_t> compiled_tiles(const Sim &s) {
+    if (s.flags & KBWG_FLAG_EXACT_ORDER) return {(uint32_t)(s.prec ? TileCfg<double>::K : TileCfg<float>::K)};
+    if (ff_capable(s)) return {(uint32_t)TileCfgFF::K, 12u};
+    if (s.prec) return {(uint32_t)TileCfg<double>::K, 11u};
+    return {(uint32_t)TileCfg<float>::K, 12u, 11u};
+}
+
+uint32_t default_tile_k(const Sim &s) { return compiled_tiles(s)[0]; }
+
+std::vector<uint32_t> tile_options(const Sim &s) {
+    std::vector<uint32_t> out;
+    if (s.flags & KBWG_FLAG_NO_FUSION) return out;
+    for (uint32_t k : compiled_tiles(s))
+        if (k <= s.n) out.push_back(k);
+    return out;
+}
+
+// The handle's tile size: its setting when a kernel exists for it and the
+// state is at least one tile, else the default.
+static uint32_t chosen_tile(const Sim &s) {
+    if (s.tile_k)
+        for (uint32_t k : tile_options(s))
+            if (k == s.tile_k) return k;
+    return default_tile_k(s);
+}
+
+uint32_t effective_tile_k(const Sim &s) {
+    if (s.flags & KBWG_FLAG_NO_FUSION) return 0;
+    const uint32_t k = chosen_tile(s);
+    return k <= s.n ? k : 0;
+}
+
 template <class T>
 static cudaError_t run_fused_t(Sim &s, const GateDesc *gates, size_t count) {
     constexpr int K = TileCfg<T>::K, R = TileCfg<T>::R;
+    const uint32_t tk = chosen_tile(s);
+    if (tk != (uint32_t)K && !(s.flags & KBWG_FLAG_EXACT_ORDER)) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (tk == 12) return run_fused_p<FastP, 12, 4>(s, gates, count);
+            if (tk == 11) return run_fused_p<FastP, 11, 3>(s, gates, count);
+        } else {
+            if (tk == 11) return run_fused_p<Fast<T>, 11, 3>(s, gates, count);
+        }
+    }
     if (s.n < (uint32_t)K) {
         for (size_t i = 0; i < count; i++) {
             if (s.prof.on) s.prof.mark(s.stream);
@@ -491,6 +538,7 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
             s.ff_resident = true;
         }
         std::vector<GateDesc> g = ff_rewrite(gates, count);
+        if (chosen_tile(s) == 12) return run_fused_p<FF2, 12, 4>(s, g.data(), g.size());
         return run_fused_p<FF2, TileCfgFF::K, TileCfgFF::R>(s, g.data(), g.size());
     }
     return s.prec ? run_fused_t<double>(s, gates, count) : run_fused_t<float>(s, gates, count);

@@ -125,8 +125,9 @@ struct PlannedSweep {
 // diagonal gates and controls may lie anywhere) and orders each sweep's gates
 // into register-layout stages.
 // keep_order: never move a gate past another one (bit-exact mode).
+// max_gates: fusion depth, the most gates one sweep may apply.
 std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *g, size_t count,
-                                      bool keep_order = false);
+                                      bool keep_order = false, size_t max_gates = kMaxSweepGates);
 
 bool is_diagonal(uint32_t kind);
 

@@ -258,6 +258,37 @@ class DenseGB300:
         N.check(self._lib.kbwg_last_flush_stats(self._h, ctypes.byref(g), ctypes.byref(p)))
         return int(g.value), int(p.value)
 
+    # ---- sweep tuning --------------------------------------------------------
+    def tile_options(self):
+        """Tile sizes (qubits per tile) with a compiled sweep kernel, default first."""
+        buf = (ctypes.c_uint32 * 8)()
+        n = ctypes.c_size_t()
+        N.check(self._lib.kbwg_tile_options(self._h, buf, 8, ctypes.byref(n)))
+        return [int(buf[i]) for i in range(n.value)]
+
+    def set_tuning(self, tile_qubits=0, fusion_depth=0):
+        N.check(self._lib.kbwg_set_tuning(self._h, int(tile_qubits), int(fusion_depth)))
+
+    def tuning(self):
+        t = N.Tuning()
+        N.check(self._lib.kbwg_get_tuning(self._h, ctypes.byref(t)))
+        return _tuning_dict(t)
+
+    def autotune(self, circuit, reps=1):
+        """Time the circuit under every tile size x fusion depth, keep the
+        fastest for this handle (the state is left unchanged)."""
+        arr = _gate_array(circuit)
+        t = N.Tuning()
+        N.check(self._lib.kbwg_autotune(self._h, arr, len(circuit), int(reps), ctypes.byref(t)))
+        return _tuning_dict(t)
+
+
+def _tuning_dict(t):
+    return {"tile_qubits": int(t.tile_qubits), "fusion_depth": int(t.fusion_depth),
+            "source": N.TUNE_SOURCES[t.source] if t.source < len(N.TUNE_SOURCES) else int(t.source),
+            "candidates": int(t.candidates), "ms_per_run": float(t.ms_per_run),
+            "default_ms_per_run": float(t.default_ms_per_run)}
+
 
 def batch_hea_tfim(circuits, zz=1.0, x=0.5, prec="c64", fast_c128=False):
     """Energies of many hardware-efficient-ansatz circuits in one launch.
