@@ -196,6 +196,50 @@ int32_t kbwg_batch_hea_tfim(uintptr_t n_circuits, const uint32_t *num_qubits, co
                             const uint64_t *param_offset, const double *params, uintptr_t n_params, double zz,
                             double x, int32_t precision, uint32_t flags, double *energies);
 
+/* ---- whole-circuit batch entries --------------------------------------- */
+/* BatchExecution (src/quantum_execution.rs:367-427) hands the backend a whole
+ * circuit per call and gets a fresh simulator each time.  These entries do
+ * the same without a handle: a register of num_qubits qubits in |0...0>
+ * (precision and flags as for kbwg_new), the whole gate list (gates, as for
+ * kbwg_apply_gates) planned and run as one flush, then the read-out.  The
+ * register comes from a per-process pool (up to 4 registers, keyed by
+ * device, size, precision and flags) and is reset for every call, its draw
+ * generator re-seeded from KBW_SEED as QubitManager::new seeds a fresh one
+ * (:183-191); so repeated calls skip the state allocation and replay
+ * repeated circuit structures from CUDA graphs.  Pooled registers keep
+ * their device memory until kbwg_batch_release.  Safe to call from several
+ * host threads: a register serves one call at a time. */
+
+/* BatchExecution::exp_value / exp_value_native (:392-418): one <H_k> per
+ * Hamiltonian; Hamiltonian k is the strings [ham_offsets[k],
+ * ham_offsets[k+1]) of the string arrays, which are laid out as for
+ * kbwg_exp_value (offsets[] indexes paulis[] / qubits[] absolutely). */
+int32_t kbwg_batch_exp_value(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                             uintptr_t n_gates, const uint8_t *paulis, const uintptr_t *qubits,
+                             const uintptr_t *offsets, const double *coefficients, const uintptr_t *ham_offsets,
+                             uintptr_t n_hamiltonians, double *out);
+
+/* BatchExecution::sample / sample_native (:367-390): `shots` samples of the
+ * listed qubits (at least one, as do_sample asserts), arguments and output as
+ * for kbwg_sample. */
+int32_t kbwg_batch_sample(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                          uintptr_t n_gates, const uintptr_t *qubits, uintptr_t n_qubits, uintptr_t shots,
+                          const double *draws, uint64_t *states, uint64_t *counts, uintptr_t capacity,
+                          uintptr_t *n_out);
+
+/* BatchExecution::gradient (:420-426): the reference answers
+ * NativeGateUnsupported and libket falls back to the parameter-shift rule;
+ * this computes E and dE/dparams natively with the adjoint method
+ * (arguments as for kbwg_adjoint_gradient). */
+int32_t kbwg_batch_gradient(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                            uintptr_t n_gates, const int32_t *param_index, uintptr_t n_params,
+                            const uint8_t *paulis, const uintptr_t *qubits, const uintptr_t *offsets,
+                            const double *coefficients, uintptr_t n_strings, uint32_t max_checkpoints,
+                            double *energy, double *gradient);
+
+/* Free the pooled registers no call is using. */
+int32_t kbwg_batch_release(void);
+
 /* QuantumExecution::clear (src/quantum_execution.rs:161; src/dense.rs:399-406). */
 int32_t kbwg_clear(kbwg_sim *sim);
 

@@ -85,6 +85,13 @@ SIGNATURES = {
     "kbwg_profile_read": (_I32, [_P, _U64P, _DP, _DP]),
     "kbwg_transfer_bytes": (_I32, [_U64P, _U64P]),
     "kbwg_state_distance": (_I32, [_P, _P, _DP]),
+    "kbwg_batch_exp_value": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_uint8),
+                                    _UP, _UP, _DP, _UP, _U, _DP]),
+    "kbwg_batch_sample": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, _UP, _U, _U, _DP, _U64P,
+                                 _U64P, _U, _UP]),
+    "kbwg_batch_gradient": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_int32),
+                                   _U, ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, ctypes.c_uint32, _DP, _DP]),
+    "kbwg_batch_release": (_I32, []),
     "kbwg_tile_options": (_I32, [_P, ctypes.POINTER(ctypes.c_uint32), _U, _UP]),
     "kbwg_set_tuning": (_I32, [_P, ctypes.c_uint32, ctypes.c_uint32]),
     "kbwg_get_tuning": (_I32, [_P, ctypes.c_void_p]),

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1028,6 +1029,178 @@ int32_t kbwg_last_flush_stats(kbwg_sim *s, uint64_t *gates, uint64_t *passes) {
     if (gates) *gates = s->last_gates;
     if (passes) *passes = s->last_passes;
     return KBWG_OK;
+}
+
+// ---- whole-circuit batch entries ------------------------------------------------
+// BatchExecution gives every call a fresh simulator (src/quantum_execution.rs:
+// 367-418).  Here a call checks a register of the right size out of a small
+// per-process pool, resets it to |0...0> (and its draw generator to KBW_SEED,
+// as a fresh QubitManager would seed it), runs the whole gate list as one
+// flush and returns the register to the pool.  Repeated calls then skip the
+// state allocation, and circuits of a repeated structure (variational loops)
+// replay their planned sweeps from the register's CUDA-graph cache.
+namespace {
+struct PoolEntry {
+    int device = 0;
+    uintptr_t n = 0;
+    int32_t prec = 0;
+    uint32_t flags = 0;
+    kbwg_sim *sim = nullptr;
+    bool busy = false;
+    uint64_t last = 0;
+};
+std::mutex g_pool_mu;
+std::vector<PoolEntry> g_pool;
+uint64_t g_pool_clock = 0;
+constexpr size_t kPoolEntries = 4;
+
+void reseed_from_env(Sim &s) {
+    const char *seed = getenv("KBW_SEED");
+    char *end = nullptr;
+    const unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
+    if (seed && *seed && end && *end == 0) s.rng = (uint64_t)sv;
+}
+}  // namespace
+
+// A reset register for (current device, n, precision, flags); *pooled says
+// whether pool_put must hand it back (false: the pool was full of busy ones).
+static int32_t pool_get(uintptr_t n, int32_t prec, uint32_t flags, kbwg_sim **out, bool *pooled) {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    kbwg_sim *s = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        for (PoolEntry &p : g_pool)
+            if (!p.busy && p.device == dev && p.n == n && p.prec == prec && p.flags == flags) {
+                p.busy = true;
+                p.last = ++g_pool_clock;
+                s = p.sim;
+                break;
+            }
+    }
+    *pooled = s != nullptr;
+    if (s) {
+        *out = s;  // handed back by the caller's lease even if the reset fails
+        const int32_t rc = kbwg_clear(s);
+        if (rc != KBWG_OK) return rc;
+    } else {
+        kbwg_sim *victim = nullptr;
+        const int32_t rc = kbwg_new(n, prec, flags, &s);
+        if (rc != KBWG_OK) return rc;
+        {
+            std::lock_guard<std::mutex> lk(g_pool_mu);
+            if (g_pool.size() >= kPoolEntries) {  // evict the least recently used idle register
+                size_t lru = g_pool.size();
+                for (size_t i = 0; i < g_pool.size(); i++)
+                    if (!g_pool[i].busy && (lru == g_pool.size() || g_pool[i].last < g_pool[lru].last)) lru = i;
+                if (lru < g_pool.size()) {
+                    victim = g_pool[lru].sim;
+                    g_pool.erase(g_pool.begin() + (long)lru);
+                }
+            }
+            if (g_pool.size() < kPoolEntries) {
+                PoolEntry p;
+                p.device = dev;
+                p.n = n;
+                p.prec = prec;
+                p.flags = flags;
+                p.sim = s;
+                p.busy = true;
+                p.last = ++g_pool_clock;
+                g_pool.push_back(p);
+                *pooled = true;
+            }
+        }
+        if (victim) kbwg_free(victim);
+        *out = s;
+    }
+    reseed_from_env(*s);
+    return KBWG_OK;
+}
+
+static void pool_put(kbwg_sim *s, bool pooled) {
+    if (!pooled) {
+        kbwg_free(s);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (PoolEntry &p : g_pool)
+        if (p.sim == s) p.busy = false;
+}
+
+struct PoolLease {
+    kbwg_sim *sim = nullptr;
+    bool pooled = false;
+    ~PoolLease() {
+        if (sim) pool_put(sim, pooled);
+    }
+};
+
+int32_t kbwg_batch_exp_value(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                             uintptr_t n_gates, const uint8_t *paulis, const uintptr_t *qubits,
+                             const uintptr_t *offsets, const double *coefficients, const uintptr_t *ham_offsets,
+                             uintptr_t n_hamiltonians, double *out) {
+    GUARD_BEGIN
+    if (n_hamiltonians && (!ham_offsets || !out)) return fail(KBWG_EINVAL, "null argument");
+    for (uintptr_t k = 0; k < n_hamiltonians; k++)
+        if (ham_offsets[k + 1] < ham_offsets[k]) return fail(KBWG_EINVAL, "ham_offsets must not decrease");
+    PoolLease L;
+    int32_t rc = pool_get(num_qubits, precision, flags, &L.sim, &L.pooled);
+    if (rc != KBWG_OK) return rc;
+    rc = kbwg_apply_gates(L.sim, gates, n_gates);
+    for (uintptr_t k = 0; rc == KBWG_OK && k < n_hamiltonians; k++) {
+        const uintptr_t a = ham_offsets[k];
+        rc = kbwg_exp_value(L.sim, paulis, qubits, offsets ? offsets + a : nullptr,
+                            coefficients ? coefficients + a : nullptr, ham_offsets[k + 1] - a, &out[k]);
+    }
+    if (rc == KBWG_OK && !n_hamiltonians) rc = kbwg_flush(L.sim);
+    return rc;
+    GUARD_END
+}
+
+int32_t kbwg_batch_sample(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                          uintptr_t n_gates, const uintptr_t *qubits, uintptr_t n_qubits, uintptr_t shots,
+                          const double *draws, uint64_t *states, uint64_t *counts, uintptr_t capacity,
+                          uintptr_t *n_out) {
+    GUARD_BEGIN
+    if (n_qubits == 0) return fail(KBWG_EINVAL, "no qubits to sample (do_sample asserts a non-empty list)");
+    PoolLease L;
+    int32_t rc = pool_get(num_qubits, precision, flags, &L.sim, &L.pooled);
+    if (rc != KBWG_OK) return rc;
+    rc = kbwg_apply_gates(L.sim, gates, n_gates);
+    if (rc == KBWG_OK) rc = kbwg_sample(L.sim, qubits, n_qubits, shots, draws, states, counts, capacity, n_out);
+    return rc;
+    GUARD_END
+}
+
+int32_t kbwg_batch_gradient(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                            uintptr_t n_gates, const int32_t *param_index, uintptr_t n_params,
+                            const uint8_t *paulis, const uintptr_t *qubits, const uintptr_t *offsets,
+                            const double *coefficients, uintptr_t n_strings, uint32_t max_checkpoints,
+                            double *energy, double *gradient) {
+    GUARD_BEGIN
+    PoolLease L;
+    int32_t rc = pool_get(num_qubits, precision, flags, &L.sim, &L.pooled);
+    if (rc != KBWG_OK) return rc;
+    return kbwg_adjoint_gradient(L.sim, gates, n_gates, param_index, n_params, paulis, qubits, offsets,
+                                 coefficients, n_strings, max_checkpoints, energy, gradient);
+    GUARD_END
+}
+
+int32_t kbwg_batch_release(void) {
+    GUARD_BEGIN
+    std::vector<kbwg_sim *> idle;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        for (size_t i = g_pool.size(); i-- > 0;)
+            if (!g_pool[i].busy) {
+                idle.push_back(g_pool[i].sim);
+                g_pool.erase(g_pool.begin() + (long)i);
+            }
+    }
+    for (kbwg_sim *s : idle) kbwg_free(s);
+    return KBWG_OK;
+    GUARD_END
 }
 
 static void fill_tuning(const Sim &s, kbwg_tuning *out) {

@@ -312,6 +312,66 @@ def batch_hea_tfim(circuits, zz=1.0, x=0.5, prec="c64", fast_c128=False):
     return out[:nc]
 
 
+def _flags(fast_c128=False, exact_order=False):
+    return (N.FLAG_FAST_C128 if fast_c128 else 0) | (N.FLAG_EXACT_ORDER if exact_order else 0)
+
+
+def batch_exp_value(num_qubits, circuit, hamiltonians, prec="c128", fast_c128=False, exact_order=False):
+    """BatchExecution::exp_value: <H_k> for each Hamiltonian after the whole
+    circuit on a fresh (pooled) register."""
+    lib = N.load()
+    ga = _gate_array(circuit)
+    allh = [s for h in hamiltonians for s in h]
+    pa, qa, oa, ca, _ = _ham_arrays(allh)
+    ho = np.ascontiguousarray(np.cumsum([0] + [len(h) for h in hamiltonians]), dtype=np.uintp)
+    out = np.zeros(max(len(hamiltonians), 1), np.float64)
+    N.check(lib.kbwg_batch_exp_value(int(num_qubits), _DT[prec][0], _flags(fast_c128, exact_order), ga, len(circuit),
+                                     _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t), _p(oa, ctypes.c_size_t),
+                                     _p(ca, ctypes.c_double), _p(ho, ctypes.c_size_t), len(hamiltonians),
+                                     _p(out, ctypes.c_double)))
+    return out[: len(hamiltonians)]
+
+
+def batch_sample(num_qubits, circuit, qubits, shots, draws=None, prec="c128", fast_c128=False, exact_order=False):
+    """BatchExecution::sample: histogram of `shots` samples after the whole
+    circuit on a fresh (pooled) register."""
+    lib = N.load()
+    ga = _gate_array(circuit)
+    q = _sizes(qubits)
+    shots = int(shots)
+    d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
+    if d is not None and d.size < shots:
+        raise ValueError("one draw per shot is needed")
+    st = np.zeros(max(shots, 1), np.uint64)
+    ct = np.zeros(max(shots, 1), np.uint64)
+    n = ctypes.c_size_t()
+    N.check(lib.kbwg_batch_sample(int(num_qubits), _DT[prec][0], _flags(fast_c128, exact_order), ga, len(circuit),
+                                  _p(q, ctypes.c_size_t), q.size, shots, None if d is None else _p(d, ctypes.c_double),
+                                  _p(st, ctypes.c_uint64), _p(ct, ctypes.c_uint64), max(shots, 1), ctypes.byref(n)))
+    return st[: n.value], ct[: n.value]
+
+
+def batch_gradient(num_qubits, circuit, param_index, n_params, hamiltonian, prec="c128", fast_c128=False,
+                   max_checkpoints=16):
+    """BatchExecution::gradient, native: E and dE/dparams by the adjoint method."""
+    lib = N.load()
+    ga = _gate_array(circuit)
+    pi = np.ascontiguousarray(param_index, dtype=np.int32)
+    pa, qa, oa, ca, ns = _ham_arrays(hamiltonian)
+    e = ctypes.c_double()
+    g = np.zeros(max(int(n_params), 1), np.float64)
+    N.check(lib.kbwg_batch_gradient(int(num_qubits), _DT[prec][0], _flags(fast_c128), ga, len(circuit),
+                                    _p(pi, ctypes.c_int32), int(n_params), _p(pa, ctypes.c_uint8),
+                                    _p(qa, ctypes.c_size_t), _p(oa, ctypes.c_size_t), _p(ca, ctypes.c_double), ns,
+                                    int(max_checkpoints), ctypes.byref(e), _p(g, ctypes.c_double)))
+    return e.value, g[: int(n_params)]
+
+
+def batch_release():
+    """Free the registers the batch entries keep between calls."""
+    N.check(N.load().kbwg_batch_release())
+
+
 def _gate_array(circuit):
     arr = (N.Gate * max(len(circuit), 1))()
     for i, (kind, t, ctrl, ang) in enumerate(circuit):
