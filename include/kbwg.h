@@ -307,7 +307,9 @@ int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
  * variables KBWG_TILE_QUBITS and KBWG_FUSION_DEPTH set them for every handle
  * kbwg_new creates (kbwg_new fails with KBWG_EINVAL on a value no kernel
  * exists for); a tile size larger than a handle's qubit count falls back to
- * the default on that handle.  They apply wherever gates are applied to a
+ * the default on that handle.  The default tile is the arithmetic's
+ * (complex64 13, complex128 12, float-float 11 qubits), or for a smaller
+ * register the largest compiled size that fits it.  They apply wherever gates are applied to a
  * handle's state (gate calls, the forward pass of kbwg_adjoint_gradient, the
  * circuit runs of kbwg_param_shift_gradient), not to the adjoint's reverse
  * sweeps or to the batch and reduction kernels. */

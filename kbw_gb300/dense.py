@@ -98,13 +98,7 @@ class DenseGB300:
 
     def apply(self, circuit):
         """Queue a list of (kind, target, controls, angle) gates in one call."""
-        arr = (N.Gate * max(len(circuit), 1))()
-        for i, (kind, t, ctrl, ang) in enumerate(circuit):
-            m = 0
-            for c in ctrl:
-                m |= 1 << int(c)
-            arr[i] = N.Gate(int(kind), int(t), m, float(ang))
-        N.check(self._lib.kbwg_apply_gates(self._h, arr, len(circuit)))
+        N.check(self._lib.kbwg_apply_gates(self._h, _gate_array(circuit), len(circuit)))
 
     def flush(self):
         N.check(self._lib.kbwg_flush(self._h))
@@ -372,14 +366,36 @@ def batch_release():
     N.check(N.load().kbwg_batch_release())
 
 
+_GATE_DT = np.dtype([("kind", "<u4"), ("target", "<u4"), ("control_mask", "<u8"), ("angle", "<f8")])
+assert _GATE_DT.itemsize == ctypes.sizeof(N.Gate)
+
+
+_MASKS = {}
+
+
+def _mask(cs):
+    """Bit mask of a control list (memoised for tuples)."""
+    try:
+        return _MASKS[cs]
+    except KeyError:
+        m = _MASKS[cs] = sum(1 << int(c) for c in cs)
+        return m
+    except TypeError:  # unhashable (a list)
+        return sum(1 << int(c) for c in cs)
+
+
 def _gate_array(circuit):
-    arr = (N.Gate * max(len(circuit), 1))()
-    for i, (kind, t, ctrl, ang) in enumerate(circuit):
-        m = 0
-        for c in ctrl:
-            m |= 1 << int(c)
-        arr[i] = N.Gate(int(kind), int(t), m, float(ang))
-    return arr
+    """kbwg_gate records of a (kind, target, controls, angle) list, as a
+    ctypes array over one numpy buffer (filled column by column)."""
+    n = len(circuit)
+    buf = np.zeros(max(n, 1), _GATE_DT)
+    if n:
+        kinds, targets, ctrls, angles = zip(*circuit)
+        buf["kind"][:n] = kinds
+        buf["target"][:n] = targets
+        buf["control_mask"][:n] = [_mask(cs) for cs in ctrls]
+        buf["angle"][:n] = angles
+    return (N.Gate * max(n, 1)).from_buffer(buf)
 
 
 def _ham_arrays(hamiltonian):
@@ -401,12 +417,7 @@ def plan(num_qubits, circuit, prec="c128", exact_order=False):
     """Host planner diagnostic: list of (tile_mask, [gate indices in execution order])."""
     lib = N.load()
     n = len(circuit)
-    arr = (N.Gate * max(n, 1))()
-    for i, (kind, t, ctrl, ang) in enumerate(circuit):
-        m = 0
-        for c in ctrl:
-            m |= 1 << int(c)
-        arr[i] = N.Gate(int(kind), int(t), m, float(ang))
+    arr = _gate_array(circuit)
     order = (ctypes.c_uint32 * max(n, 1))()
     ends = (ctypes.c_uint32 * max(n, 1))()
     masks = (ctypes.c_uint64 * max(n, 1))()

@@ -39,6 +39,8 @@ def lib():
         L.od_clear.argtypes = [ctypes.c_void_p]
         L.od_gate.restype = ctypes.c_int
         L.od_gate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, sz, szp, sz]
+        L.od_apply_gates.restype = ctypes.c_int
+        L.od_apply_gates.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), szp, u64p, dp, sz]
         L.od_measure_p1.restype = ctypes.c_double
         L.od_measure_p1.argtypes = [ctypes.c_void_p, sz]
         L.od_measure_collapse.argtypes = [ctypes.c_void_p, sz, ctypes.c_int, ctypes.c_double]
@@ -190,9 +192,19 @@ class OracleDense:
         lib().od_swap_qubits(self._h, int(a), int(b))
 
     def apply(self, circuit):
-        """Apply a list of (kind, target, controls, angle) tuples."""
-        for kind, target, control, angle in circuit:
-            self.gate(kind, target, control, angle)
+        """Apply a list of (kind, target, controls, angle) tuples (one call)."""
+        n = len(circuit)
+        if n == 0:
+            return
+        kinds, targets, ctrls, angles = zip(*circuit)
+        k = np.ascontiguousarray(kinds, dtype=np.intc)
+        t = np.ascontiguousarray(targets, dtype=np.uintp)
+        m = np.ascontiguousarray([sum(1 << int(c) for c in cs) for cs in ctrls], dtype=np.uint64)
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        rc = lib().od_apply_gates(self._h, _ptr(k, ctypes.c_int), _ptr(t, ctypes.c_size_t), _ptr(m, ctypes.c_uint64),
+                                  _ptr(a, ctypes.c_double), n)
+        if rc != 0:
+            raise ValueError("oracle: bad qubit index")
 
 
 def uniform_scale(total):

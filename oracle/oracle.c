@@ -179,6 +179,18 @@ int od_gate(od_state *s, int kind, double angle, size_t target, const size_t *co
     return 0;
 }
 
+int od_apply_gates(od_state *s, const int *kinds, const size_t *targets, const uint64_t *masks,
+                   const double *angles, size_t n_gates) {
+    size_t ctrl[64];
+    for (size_t i = 0; i < n_gates; i++) {
+        size_t nc = 0;
+        for (size_t q = 0; q < 64; q++)
+            if ((masks[i] >> q) & 1u) ctrl[nc++] = q;
+        if (od_gate(s, kinds[i], angles[i], targets[i], ctrl, nc) != 0) return -1;
+    }
+    return 0;
+}
+
 double od_measure_p1(od_state *s, size_t target) {
     return s->prec ? measure_p1_f64(cur_buf(s), s->ns, target)
                    : measure_p1_f32(cur_buf(s), s->ns, target);

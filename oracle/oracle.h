@@ -50,6 +50,13 @@ void od_set_num_threads(int n);
 int od_gate(od_state *s, int kind, double angle, size_t target, const size_t *control,
             size_t n_control);
 
+/* A gate list in one call (the loop of LiveExecution::compute_gate,
+ * src/quantum_execution.rs:310-314): record i = kinds[i], targets[i],
+ * control mask masks[i], angles[i].  Returns 0, or -1 at the first bad
+ * qubit index (the gates before it stay applied). */
+int od_apply_gates(od_state *s, const int *kinds, const size_t *targets, const uint64_t *masks,
+                   const double *angles, size_t n_gates);
+
 double od_measure_p1(od_state *s, size_t target);
 void od_measure_collapse(od_state *s, size_t target, int result, double p);
 

@@ -55,16 +55,32 @@ def test_every_tile_size_and_depth_matches_oracle(arith):
     sim.close()
 
 
+def test_small_registers_default_to_the_largest_tile_that_fits():
+    # a 12-qubit register is below the complex64 default tile (13 qubits):
+    # it runs on 12-qubit tiles; float-float keeps its 11-qubit default
+    n = 12
+    for prec, ff, k in (("c64", False, 12), ("c128", True, 11)):
+        sim = DenseGB300(n, prec, fast_c128=ff)
+        assert sim.tile_options()[0] == k and sim.tuning()["tile_qubits"] == k
+        circ = C.random_circuit(n, 150, 6, max_controls=2)
+        ref = oracle.OracleDense(n, prec)
+        ref.apply(circ)
+        sim.apply(circ)
+        assert rel_err(sim.state(), ref.state()) < TOL[prec]
+        sim.close()
+    # complex64 11 qubits: 11 fits, 12 and 13 do not
+    sim = DenseGB300(11, "c64")
+    assert sim.tile_options() == [11] and sim.tuning()["tile_qubits"] == 11
+    sim.close()
+
+
 def test_tile_size_below_default_runs_fused_on_small_registers():
-    # a 12-qubit complex64 register is below the default 13-qubit tile (one
-    # kernel per gate by default); a 12- or 11-qubit tile fuses it
     n = 12
     circ = C.random_circuit(n, 200, 5, max_controls=2)
     ref = oracle.OracleDense(n, "c64")
     ref.apply(circ)
     sim = DenseGB300(n, "c64")
     assert sim.tile_options() == [12, 11]
-    assert sim.tuning()["tile_qubits"] == 0
     for k in (12, 11):
         sim.clear()
         sim.set_tuning(k, 0)
