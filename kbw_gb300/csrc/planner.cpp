@@ -73,11 +73,18 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
     // Greedy selection of a sweep's gates.  grow: the admissible high targets
     // (bits >= 5) are collected first come, first served up to max_high;
     // otherwise they are the fixed set `needed`.
+    const uint64_t all_qubits = (n >= 64) ? ~0ull : ((1ull << n) - 1);
     auto select = [&](uint64_t needed, bool grow, std::vector<size_t> *take, std::vector<size_t> *rest) {
         Deferred blocked;
         size_t taken = 0;
-        const size_t scan = std::min(remaining.size(), window);
+        size_t scan = std::min(remaining.size(), window);
         for (size_t ii = 0; ii < scan; ii++) {
+            // every qubit is a deferred non-diagonal target: no later gate can pass
+            if ((blocked.ndt & all_qubits) == all_qubits || blocked.all || taken >= max_gates) {
+                if (rest)
+                    for (size_t jj = ii; jj < scan; jj++) rest->push_back(remaining[jj]);
+                break;
+            }
             const size_t i = remaining[ii];
             const GateDesc &x = g[i];
             bool ok = blocked.passes(x) && taken < max_gates;
