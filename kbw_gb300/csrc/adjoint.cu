@@ -552,12 +552,9 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
                                    size_t hi, int num_sms) {
     using AK = AdjKernel<P, K, R>;
     using Mem = typename P::Mem;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_adjoint<P, K, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AK::kSmem);
+    {
+        const cudaError_t e = ensure_smem_limit((const void *)k_adjoint<P, K, R>, AK::kSmem);
         if (e != cudaSuccess) return e;
-        attr = true;
     }
     // reverse list of inverse gates; gradient info follows each gate through the planner
     std::vector<GateDesc> rev;
@@ -644,11 +641,9 @@ static cudaError_t apply_hamiltonian_tiled(Sim &s, void *lam, const std::vector<
     const std::vector<PauliPass> passes = plan_pauli_passes(s.n, K, xm, kMaxTerms, wide);
     if (!wide.empty()) return cudaSuccess;
     const size_t smem = (sizeof(cx<T>) << K) + (sizeof(uint64_t) << (K - kLaneBits));
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_apply_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        const cudaError_t e = ensure_smem_limit((const void *)k_apply_tile<T>, smem);
         if (e != cudaSuccess) return e;
-        attr = true;
     }
     const uint64_t tiles = 1ull << (s.n - K);
     const unsigned grid = (unsigned)std::min<uint64_t>(tiles, 152ull * 8);

@@ -5,7 +5,10 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace kbwg {
 
@@ -26,6 +29,30 @@ inline cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemc
     if (kind == cudaMemcpyHostToDevice) g_h2d_bytes.fetch_add(bytes, std::memory_order_relaxed);
     if (kind == cudaMemcpyDeviceToHost) g_d2h_bytes.fetch_add(bytes, std::memory_order_relaxed);
     return cudaMemcpyAsync(dst, src, bytes, kind, s);
+}
+
+// Raise a kernel's dynamic shared-memory limit once per device (the setting
+// belongs to the device's context), safely from any host thread.
+inline cudaError_t ensure_smem_limit(const void *func, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto &d : done)
+        if (d.first == dev && d.second == func) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done.emplace_back(dev, func);
+    return e;
+}
+
+// Number of SMs of the current device.
+inline cudaError_t current_sm_count(int &sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return e;
 }
 
 // One gate as the kernels see it.  Constants are pre-computed on the host in

@@ -228,18 +228,11 @@ template <class P, int K, int R>
 static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     using SK = SweepKernel<P, K, R>;
     using Mem = typename P::Mem;
-    static bool attr_set = false;
-    static int num_sms = 0;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_sweep<P, K, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)SK::kSmem);
+    int num_sms = 0;
+    {
+        cudaError_t e = ensure_smem_limit((const void *)k_sweep<P, K, R>, SK::kSmem);
+        if (e == cudaSuccess) e = current_sm_count(num_sms);
         if (e != cudaSuccess) return e;
-        int dev = 0;
-        e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
     }
     const void *kid = (const void *)k_sweep<P, K, R>;
     const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
