@@ -312,6 +312,32 @@ def test_28q_brickwork_round_trip(prec):
     assert st[0] == 0 and abs(re[0] - 1.0) < tol
 
 
+@pytest.mark.parametrize("n,prec,fast", [(32, "c64", False), (31, "c128", True)])
+def test_largest_registers(n, prec, fast):
+    """The largest registers (32 GiB of amplitudes; 32 qubits is the Dense
+    limit): a random circuit with controls on the top qubits keeps the norm,
+    its inverse returns |0...0>, and a Bell pair between the top and bottom
+    qubit reads out exactly (dump, p1, measurement with injected draws)."""
+    circ = C.random_circuit(n, 120, 77, max_controls=2)
+    inv = [(k, t, c, -a if k in C.PARAMETRIC else a) for (k, t, c, a) in reversed(circ)]
+    sim = DenseGB300(n, prec, fast_c128=fast)
+    tol = 1e-12 if prec == "c128" else 2e-5
+    sim.apply(circ)
+    assert abs(sim.exp_value([(1.0, [])]) - 1.0) < tol
+    sim.apply(inv)
+    top = n - 1
+    assert sim.measure_p1(top) < tol and sim.measure_p1(0) < tol
+    sim.clear()
+    sim.hadamard(top)
+    sim.pauli_x(0, [top])
+    st, re, im = sim.dump([top, 0])
+    assert st.tolist() == [0, 3]
+    assert np.allclose(re, [2 ** -0.5] * 2, atol=tol) and np.allclose(im, 0.0, atol=tol)
+    assert abs(sim.measure_p1(top) - 0.5) < tol
+    assert sim.measure([top, 0], [0.75, 0.1]) in (0, 3)
+    sim.close()
+
+
 # ---- complex128 float-float fast path ------------------------------------------
 
 @pytest.mark.parametrize("n,gates,seed", [(12, 300, 61), (16, 500, 62), (20, 800, 63), (23, 400, 64)])
