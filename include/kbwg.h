@@ -298,6 +298,14 @@ int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative);
 /* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
 int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
 
+/* Failure-path check without a GPU fault: queued gates are flushed, then one
+ * CTA runs the bounded wait every tile kernel uses for its TMA copies, on a
+ * barrier that nothing completes, for `spins` polls (1..2^22).  The polls run
+ * out, the kernel sets the handle's error flag and returns, and the call
+ * reports it as any tile kernel's timeout is reported: KBWG_ETIMEOUT.  The
+ * state is untouched and the handle stays usable. */
+int32_t kbwg_wait_probe(kbwg_sim *sim, uint32_t spins);
+
 /* ---- sweep tuning (no counterpart in the reference) ---------------------- */
 
 /* Gate calls run as fused sweeps (one pass over the state applies many

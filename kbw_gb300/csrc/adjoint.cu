@@ -426,16 +426,7 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
     for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
         const uint64_t base = tile_base(tau);
-        bool ok = false;
-        for (uint32_t spin = 0; spin < (1u << 22); spin++)
-            if (mbar_try_wait(bar, it & 1u)) {
-                ok = true;
-                break;
-            }
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicExch(p.err, 1);
-            return;
-        }
+        if (!tile_wait(bar, it & 1u, p.err)) return;
         Amp vp[NR], vl[NR];
         int layout = p.stage_layout[0];
         int R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);

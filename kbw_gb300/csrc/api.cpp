@@ -1024,6 +1024,16 @@ int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h) {
     return KBWG_OK;
 }
 
+int32_t kbwg_wait_probe(kbwg_sim *s, uint32_t spins) {
+    GUARD_BEGIN
+    ENTER(s);
+    if (spins == 0 || spins > (1u << 22)) return fail(KBWG_EINVAL, "spins must be 1..2^22");
+    CUDA_TRY(flush_queue(*s));
+    CUDA_TRY(launch_wait_probe(s->d_err, spins, s->stream));
+    return check_device_error(s);
+    GUARD_END
+}
+
 int32_t kbwg_last_flush_stats(kbwg_sim *s, uint64_t *gates, uint64_t *passes) {
     if (!s) return fail(KBWG_EINVAL, "null handle");
     if (gates) *gates = s->last_gates;

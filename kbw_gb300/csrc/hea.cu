@@ -440,17 +440,8 @@ __global__ void __launch_bounds__(HeaKernel<P, K, R>::kThreads, (sizeof(typename
                                 tma_load(tile_mem + (size_t)c * chunk, slot + base + chunk_off[c],
                                          chunk * (uint32_t)sizeof(Mem), bar);
                         }
-                        bool ok = false;
-                        for (uint32_t spin = 0; spin < (1u << 22); spin++)
-                            if (mbar_try_wait(bar, phase & 1u)) {
-                                ok = true;
-                                break;
-                            }
+                        if (!tile_wait(bar, phase & 1u, a.err)) return;
                         phase++;
-                        if (__syncthreads_or(!ok)) {
-                            if (threadIdx.x == 0) atomicExch(a.err, 1);
-                            return;
-                        }
 #pragma unroll
                         for (int j = 0; j < NR; j++) v[j] = P::from_mem(tile_mem[F | ((uint32_t)j << R0)]);
                     }

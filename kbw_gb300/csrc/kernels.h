@@ -37,6 +37,8 @@ template <class T> cudaError_t launch_init(void *st, uint32_t n, cudaStream_t s)
 // complex128 storage: binary64 -> float-float pairs (to_ff) or back, in place.
 cudaError_t launch_ff_convert(void *st, uint32_t n, bool to_ff, cudaStream_t s);
 cudaError_t launch_init_ff(void *st, uint32_t n, cudaStream_t s);
+// One CTA runs the tile kernels' bounded wait on a barrier nothing completes.
+cudaError_t launch_wait_probe(int *err, uint32_t spins, cudaStream_t s);
 template <class T> cudaError_t launch_swap(void *st, uint32_t n, uint32_t a, uint32_t b, cudaStream_t s);
 
 // Sum of |a_s|^2 over s with (s & M) == V, FP64 result in scratch.result[0].

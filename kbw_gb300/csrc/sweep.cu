@@ -106,16 +106,7 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
     const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
     for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
         const uint32_t base = tile_base(tau);
-        bool ok = false;
-        for (uint32_t spin = 0; spin < (1u << 22); spin++)
-            if (mbar_try_wait(bar, it & 1u)) {
-                ok = true;
-                break;
-            }
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicExch(p.err, 1);
-            return;
-        }
+        if (!tile_wait(bar, it & 1u, p.err)) return;
         Amp v[NR];
         int layout = p.stage_layout[0];
         int R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
@@ -152,6 +143,25 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
             st[base + chunk_off[u >> l] + (u & lowmask)] = P::to_mem(v[j]);
         }
     }
+}
+
+// Diagnostic of the failure path: one CTA waits through tile_wait on an
+// mbarrier nothing arrives on, so its polls run out and it sets the error
+// flag and returns, as a tile kernel whose copies never completed would.
+__global__ void k_wait_probe(int *err, uint32_t spins) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    tile_wait(&bar, 0, err, spins);
+}
+
+cudaError_t launch_wait_probe(int *err, uint32_t spins, cudaStream_t s) {
+    k_wait_probe<<<1, 64, 0, s>>>(err, spins);
+    count_launch();
+    return cudaGetLastError();
 }
 
 // ---- replay cache ------------------------------------------------------------------

@@ -34,6 +34,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Every thread of the CTA waits for phase `parity` of a TMA mbarrier with a
+// bounded number of polls (the only wait the tile kernels have).  If any
+// thread's polls run out, thread 0 sets *err (the host turns it into
+// KBWG_ETIMEOUT), the threads that gave up poll once more, again bounded, so
+// that the copies they waited for can land before the CTA releases its
+// shared memory, and every thread gets false: the caller returns.
+__device__ __forceinline__ bool tile_wait(uint64_t *bar, uint32_t parity, int *err, uint32_t spins = 1u << 22) {
+    bool ok = false;
+    for (uint32_t spin = 0; spin < spins; spin++)
+        if (mbar_try_wait(bar, parity)) {
+            ok = true;
+            break;
+        }
+    if (!__syncthreads_or(!ok)) return true;
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    for (uint32_t spin = 0; !ok && spin < spins; spin++) ok = mbar_try_wait(bar, parity);
+    return false;
+}
 __device__ __forceinline__ void tma_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_addr(dst)),

@@ -252,6 +252,11 @@ class DenseGB300:
         N.check(self._lib.kbwg_last_flush_stats(self._h, ctypes.byref(g), ctypes.byref(p)))
         return int(g.value), int(p.value)
 
+    def wait_probe(self, spins=1024):
+        """Run the tile kernels' bounded wait on a barrier nothing completes;
+        raises KbwgError with code ETIMEOUT (the handle stays usable)."""
+        N.check(self._lib.kbwg_wait_probe(self._h, int(spins)))
+
     # ---- sweep tuning --------------------------------------------------------
     def tile_options(self):
         """Tile sizes (qubits per tile) with a compiled sweep kernel, default first."""
