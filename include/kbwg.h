@@ -295,6 +295,12 @@ int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h);
  * reduction on a's device; both handles must live on the same device). */
 int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative);
 
+/* State fidelity |<a|b>|^2 / (<a|a> <b|b>) of two handles of equal size on
+ * the same device, of either precision (FP64 on-device reduction): the error
+ * statement of a complex64 run against a complex128 run of the same circuit
+ * (infidelity = 1 - fidelity). */
+int32_t kbwg_state_fidelity(kbwg_sim *a, kbwg_sim *b, double *fidelity);
+
 /* Passes (kernel sweeps or single-gate kernels) used by the last flush. */
 int32_t kbwg_last_flush_stats(kbwg_sim *sim, uint64_t *gates, uint64_t *passes);
 

@@ -86,6 +86,7 @@ SIGNATURES = {
     "kbwg_profile_read": (_I32, [_P, _U64P, _DP, _DP]),
     "kbwg_transfer_bytes": (_I32, [_U64P, _U64P]),
     "kbwg_state_distance": (_I32, [_P, _P, _DP]),
+    "kbwg_state_fidelity": (_I32, [_P, _P, _DP]),
     "kbwg_batch_exp_value": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_uint8),
                                     _UP, _UP, _DP, _UP, _U, _DP]),
     "kbwg_batch_sample": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, _UP, _U, _U, _DP, _U64P,

@@ -1018,6 +1018,24 @@ int32_t kbwg_state_distance(kbwg_sim *a, kbwg_sim *b, double *relative) {
     GUARD_END
 }
 
+int32_t kbwg_state_fidelity(kbwg_sim *a, kbwg_sim *b, double *fidelity) {
+    GUARD_BEGIN
+    if (!a || !b || !fidelity) return fail(KBWG_EINVAL, "null argument");
+    if (a->n != b->n || a->device != b->device) return fail(KBWG_EINVAL, "handles differ in size or device");
+    ENTER(a);
+    CUDA_TRY(settle(*a));
+    CUDA_TRY(settle(*b));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(launch_overlap(a->state, a->prec, b->state, b->prec, a->n, a->rs, a->stream));
+    CUDA_TRY(copy_async(a->h_result, a->rs.result, 4 * sizeof(double), cudaMemcpyDeviceToHost, a->stream));
+    CUDA_TRY(cudaStreamSynchronize(a->stream));
+    const double *r = a->h_result;
+    const double den = r[2] * r[3];
+    *fidelity = den > 0.0 ? (r[0] * r[0] + r[1] * r[1]) / den : 0.0;
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_transfer_bytes(uint64_t *h2d, uint64_t *d2h) {
     if (h2d) *h2d = g_h2d_bytes.load();
     if (d2h) *d2h = g_d2h_bytes.load();

@@ -49,6 +49,9 @@ cudaError_t launch_masked_norm(const void *st, uint32_t n, uint64_t M, uint64_t 
 // sum |a - b|^2 into scratch.result[0] and sum |b|^2 into result[1].
 template <class T>
 cudaError_t launch_distance(const void *a, const void *b, uint32_t n, const ReduceScratch &rs, cudaStream_t s);
+// Re<a|b>, Im<a|b>, <a|a>, <b|b> into rs.result[0..3]; prec_*: 0 complex64, 1 complex128.
+cudaError_t launch_overlap(const void *a, int prec_a, const void *b, int prec_b, uint32_t n, const ReduceScratch &rs,
+                           cudaStream_t s);
 
 // One step of the sequential measurement: conditional p1 of ctl->qubit[step]
 // given the outcomes so far, then the WeightedIndex decision, all on device.

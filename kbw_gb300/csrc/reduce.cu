@@ -245,6 +245,65 @@ cudaError_t launch_distance(const void *a, const void *b, uint32_t n, const Redu
 template cudaError_t launch_distance<float>(const void *, const void *, uint32_t, const ReduceScratch &, cudaStream_t);
 template cudaError_t launch_distance<double>(const void *, const void *, uint32_t, const ReduceScratch &, cudaStream_t);
 
+// partials: Re<a|b>, Im<a|b>, <a|a>, <b|b> (four values per block), either
+// precision on either side, accumulated in FP64.
+template <class TA, class TB>
+__global__ void __launch_bounds__(kReduceThreads)
+    k_overlap(const cx<TA> *__restrict__ a, const cx<TB> *__restrict__ b, uint64_t count, ReduceScratch rs) {
+    AccD re, im, na, nb;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const cx<TA> x = a[i];
+        const cx<TB> y = b[i];
+        const double ar = x.re, ai = x.im, br = y.re, bi = y.im;
+        re.add_prod(ar, br);  // conj(a) b = (ar br + ai bi) + i (ar bi - ai br)
+        re.add_prod(ai, bi);
+        im.add_prod(ar, bi);
+        im.add_prod_neg(ai, br);
+        na.add_prod(ar, ar);
+        na.add_prod(ai, ai);
+        nb.add_prod(br, br);
+        nb.add_prod(bi, bi);
+    }
+    const double v0 = block_sum(re.value());
+    const double v1 = block_sum(im.value());
+    const double v2 = block_sum(na.value());
+    const double v3 = block_sum(nb.value());
+    if (threadIdx.x == 0) {
+        rs.partials[4 * blockIdx.x] = v0;
+        rs.partials[4 * blockIdx.x + 1] = v1;
+        rs.partials[4 * blockIdx.x + 2] = v2;
+        rs.partials[4 * blockIdx.x + 3] = v3;
+    }
+    if (last_block(rs.ticket)) {
+        double t[4];
+        for (int k = 0; k < 4; k++) t[k] = sum_partials(rs.partials, gridDim.x, 4, k);
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < 4; k++) rs.result[k] = t[k];
+            *rs.ticket = 0;
+        }
+    }
+}
+
+cudaError_t launch_overlap(const void *a, int prec_a, const void *b, int prec_b, uint32_t n, const ReduceScratch &rs,
+                           cudaStream_t s) {
+    const uint64_t count = 1ull << n;
+    if (prec_a && prec_b)
+        k_overlap<double, double><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<double> *)a,
+                                                                           (const cx<double> *)b, count, rs);
+    else if (prec_a)
+        k_overlap<double, float><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<double> *)a,
+                                                                          (const cx<float> *)b, count, rs);
+    else if (prec_b)
+        k_overlap<float, double><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<float> *)a,
+                                                                          (const cx<double> *)b, count, rs);
+    else
+        k_overlap<float, float><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<float> *)a, (const cx<float> *)b,
+                                                                         count, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ---- sequential measurement step ------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(kReduceThreads)

@@ -246,6 +246,13 @@ class DenseGB300:
         N.check(self._lib.kbwg_state_distance(self._h, other._h, ctypes.byref(out)))
         return out.value
 
+    def fidelity(self, other):
+        """|<self|other>|^2 / (<self|self><other|other>), on the device; the
+        two handles may differ in precision."""
+        out = ctypes.c_double()
+        N.check(self._lib.kbwg_state_fidelity(self._h, other._h, ctypes.byref(out)))
+        return out.value
+
     def last_flush_stats(self):
         g = ctypes.c_uint64()
         p = ctypes.c_uint64()

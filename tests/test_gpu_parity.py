@@ -453,6 +453,28 @@ def test_fast_c128_distance_and_gradient_after_gates():
     assert abs(a.state()[0] - 1.0) < 1e-15
 
 
+def test_state_fidelity_across_precisions():
+    """kbwg_state_fidelity against numpy on the host copies, for every pair
+    of arithmetics (complex64, binary64 complex128, float-float complex128)."""
+    n = 15
+    circ = C.random_circuit(n, 250, 91, max_controls=2)
+    other = C.random_circuit(n, 40, 92)
+    sims = {"c64": DenseGB300(n, "c64"), "c128": DenseGB300(n, "c128"),
+            "ff": DenseGB300(n, "c128", fast_c128=True)}
+    for s in sims.values():
+        s.apply(circ)
+    sims["c128"].apply(other)  # a different state for the off-diagonal pairs
+    host = {k: s.state().astype(np.complex128) for k, s in sims.items()}
+    for ka, a in sims.items():
+        for kb, b in sims.items():
+            x, y = host[ka], host[kb]
+            want = abs(np.vdot(x, y)) ** 2 / (np.vdot(x, x).real * np.vdot(y, y).real)
+            got = a.fidelity(b)
+            assert abs(got - want) < 1e-12, (ka, kb, got, want)
+    assert 1 - sims["c64"].fidelity(sims["ff"]) < 1e-10
+    assert 1 - sims["ff"].fidelity(sims["ff"]) < 1e-14
+
+
 @pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", True), ("c128", False)])
 def test_graph_replay_same_structure_new_angles(prec, fast):
     """Repeated flushes of one gate structure replay a CUDA graph with freshly
