@@ -362,11 +362,12 @@ def run_grover_bench(args, torch, DenseGB300, C):
 def run_gate_classes(args):
     """Per gate class: CUDA-event time of the sweeps that apply 32 gates of
     one class (first row: a single RZ, the memory-pass floor of a sweep);
-    us_per_gate = sweep time / gates."""
+    us_per_gate = sweep time / gates.  Runs of diagonal gates are not folded
+    here, so each of the 32 gates is applied."""
     from kbw_gb300 import DenseGB300
     from kbw_gb300 import circuits as C
     n, prec = args.qubits, args.prec
-    sim = DenseGB300(n, prec, fast_c128=(prec == "c128" and args.arith == "ff"))
+    sim = DenseGB300(n, prec, fast_c128=(prec == "c128" and args.arith == "ff"), fold=False)
     cases = [("one RZ (memory pass)", [(C.RZ, 3, (), 0.3)]),
              ("32 RY on a register qubit", [(C.RY, 8, (), 0.1 * i) for i in range(32)]),
              ("32 RX on a register qubit", [(C.RX, 8, (), 0.1 * i) for i in range(32)]),

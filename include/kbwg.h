@@ -68,7 +68,9 @@ enum {
                                       ~48-bit significand, < 1e-12 relative to binary64) */
     KBWG_FLAG_EXACT_ORDER = 1u << 2, /* fuse without reordering commuting gates: amplitudes then
                                         equal the reference's bit for bit */
-    KBWG_FLAG_NO_GRAPHS = 1u << 3    /* do not replay repeated gate structures from CUDA graphs */
+    KBWG_FLAG_NO_GRAPHS = 1u << 3,   /* do not replay repeated gate structures from CUDA graphs */
+    KBWG_FLAG_NO_FOLD = 1u << 4      /* do not fold runs of diagonal one-qubit gates on a qubit into one
+                                        (per-gate cost measurements) */
 };
 
 /* QuantumExecution::new (src/quantum_execution.rs:53; src/dense.rs:70-89).

@@ -16,6 +16,7 @@ FLAG_NO_FUSION = 1
 FLAG_FAST_C128 = 2
 FLAG_EXACT_ORDER = 4
 FLAG_NO_GRAPHS = 8
+FLAG_NO_FOLD = 16
 
 
 class KbwgError(RuntimeError):

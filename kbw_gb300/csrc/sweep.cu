@@ -541,7 +541,7 @@ cudaError_t init_state(Sim &s) {
 
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
     std::vector<GateDesc> folded;
-    if (!(s.flags & KBWG_FLAG_EXACT_ORDER)) {
+    if (!(s.flags & (KBWG_FLAG_EXACT_ORDER | KBWG_FLAG_NO_FOLD))) {
         folded = fold_diagonals(gates, count);
         gates = folded.data();
         count = folded.size();

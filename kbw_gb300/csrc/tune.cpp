@@ -44,7 +44,8 @@ uint64_t structure_hash(const std::vector<GateDesc> &g) {
 }
 
 Key key_of(const Sim &s, const std::vector<GateDesc> &g) {
-    const uint32_t arith = s.flags & (KBWG_FLAG_FAST_C128 | KBWG_FLAG_EXACT_ORDER | KBWG_FLAG_NO_FUSION);
+    const uint32_t arith =
+        s.flags & (KBWG_FLAG_FAST_C128 | KBWG_FLAG_EXACT_ORDER | KBWG_FLAG_NO_FUSION | KBWG_FLAG_NO_FOLD);
     return Key(s.device, s.n, s.prec, arith, structure_hash(g));
 }
 

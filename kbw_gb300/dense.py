@@ -32,7 +32,8 @@ def _p(a, t):
 class DenseGB300:
     """One state vector of 2^n amplitudes on the current CUDA device."""
 
-    def __init__(self, num_qubits, prec="c128", fusion=True, fast_c128=False, exact_order=False, graphs=True):
+    def __init__(self, num_qubits, prec="c128", fusion=True, fast_c128=False, exact_order=False, graphs=True,
+                 fold=True):
         lib = N.load()
         if prec not in _DT:
             raise ValueError("prec must be 'c64' or 'c128'")
@@ -41,6 +42,7 @@ class DenseGB300:
         flags = (0 if fusion else N.FLAG_NO_FUSION) | (N.FLAG_FAST_C128 if fast_c128 else 0)
         flags |= N.FLAG_EXACT_ORDER if exact_order else 0
         flags |= 0 if graphs else N.FLAG_NO_GRAPHS
+        flags |= 0 if fold else N.FLAG_NO_FOLD
         h = ctypes.c_void_p()
         N.check(lib.kbwg_new(self.num_qubits, _DT[prec][0], flags, ctypes.byref(h)))
         self._h = h

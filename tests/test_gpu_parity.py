@@ -525,8 +525,10 @@ def test_folded_diagonal_chains(prec, fast):
         else:  # non-diagonal on q: closes the run
             kind = [C.H, C.RX, C.RY, C.Y][int(rng.integers(0, 4))]
             circ.append((kind, q, (), float(rng.uniform(0, 2 * math.pi))))
-    sim = DenseGB300(n, prec, fast_c128=fast)
-    sim.apply(circ)
     ref = oracle.OracleDense(n, prec)
     ref.apply(circ)
-    assert rel_err(sim.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
+    for fold in (True, False):  # KBWG_FLAG_NO_FOLD applies every gate as given
+        sim = DenseGB300(n, prec, fast_c128=fast, fold=fold)
+        sim.apply(circ)
+        assert rel_err(sim.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
+        sim.close()
