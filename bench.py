@@ -643,7 +643,8 @@ def main():
     ap.add_argument("--adj-qubits", type=int, default=24)
     ap.add_argument("--adj-layers", type=int, default=10)
     ap.add_argument("--adj-reps", type=int, default=3)
-    ap.add_argument("--adj-ps-c128", action="store_true", help="also time parameter shift in float-float complex128")
+    ap.add_argument("--no-adj-ps-c128", dest="adj_ps_c128", action="store_false",
+                    help="skip the float-float complex128 parameter-shift timing")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu DRAM bytes (read + write) per sweep launch; default: the 25-qubit capture "
                          "of k_sweep<FF2> (1017.4 MB) scaled by the amplitude count")
