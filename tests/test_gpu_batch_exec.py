@@ -100,3 +100,14 @@ def test_batch_errors_and_release():
     batch_release()
     assert np.array_equal(batch_exp_value(12, circ, [C.tfim_ring(12)]), first)
     batch_release()
+
+
+def test_batch_empty_circuit_and_no_hamiltonians():
+    # no gates: <H> of |0...0>; no Hamiltonians: nothing to return
+    n = 12
+    got = batch_exp_value(n, [], [[(1.0, [(C.PAULI_Z, 3)])], [(2.0, [(C.PAULI_X, 0)])]])
+    assert got.tolist() == [1.0, 0.0]
+    assert batch_exp_value(n, C.random_circuit(n, 20, 3), []).shape == (0,)
+    st, ct = batch_sample(n, [], [0, 5], 16, C.uniform_draws(16, 2))
+    assert st.tolist() == [0] and ct.tolist() == [16]
+    batch_release()

@@ -473,6 +473,8 @@ def test_state_fidelity_across_precisions():
             assert abs(got - want) < 1e-12, (ka, kb, got, want)
     assert 1 - sims["c64"].fidelity(sims["ff"]) < 1e-10
     assert 1 - sims["ff"].fidelity(sims["ff"]) < 1e-14
+    with pytest.raises(KbwgError):
+        sims["c64"].fidelity(DenseGB300(n - 1, "c64"))
 
 
 @pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", True), ("c128", False)])

@@ -157,3 +157,22 @@ def test_environment_overrides(monkeypatch):
     with pytest.raises(KbwgError) as ei:
         DenseGB300(n, "c64")
     assert ei.value.code == N.EINVAL
+
+
+def test_autotune_on_registers_below_every_tile():
+    # 8 qubits: no compiled tile fits, the handle runs one kernel per gate;
+    # the tuner has nothing to choose and says so without timing
+    n = 8
+    circ = C.random_circuit(n, 60, 12, max_controls=1)
+    sim = DenseGB300(n, "c64")
+    assert sim.tile_options() == []
+    t = sim.autotune(circ)
+    assert t["tile_qubits"] == 0 and t["candidates"] == 0 and t["source"] == "default"
+    sim.apply(circ)
+    ref = oracle.OracleDense(n, "c64")
+    ref.apply(circ)
+    assert rel_err(sim.state(), ref.state()) < TOL["c64"]
+    with pytest.raises(KbwgError) as ei:
+        sim.set_tuning(11, 0)
+    assert ei.value.code == N.EINVAL
+    sim.close()
