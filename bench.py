@@ -14,6 +14,9 @@ the measured HBM copy bandwidth.
 e2e: the same metric through the C ABI with host buffers: per step the state
 is cleared, every gate is submitted by its own trait call, then <Z_i> for all
 qubits and one full-register measurement (host draws) are read back.
+Before the warm-up the engine's autotuner times the compiled tile sizes and
+fusion depths on the circuit and keeps the fastest (config.tuning;
+--no-tune keeps the defaults).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
