@@ -122,15 +122,35 @@ __global__ void __launch_bounds__(256) k_apply_tile(const cx<T> *__restrict__ ph
             tile[u] = phi[base + chunk_off[u >> l] + (u & lowmask)];
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x) {
-            T ar = 0, ai = 0;
+            // strings without flips and with a real factor (Z-type) only add
+            // their signed coefficient to d, applied once to the amplitude;
+            // real-factor strings with flips take two FMAs, the rest four
+            // (the branches are uniform: they depend on the term only)
+            T ar = 0, ai = 0, d = 0;
             for (uint32_t k = 0; k < p.nterms; k++) {
                 const ApplyTileTerm &t = p.t[k];
                 const uint32_t src = u ^ t.xl;
                 const bool neg = ((__popc(src & t.zl) + __popcll(base & t.zo)) & 1) != 0;
-                const T wr = neg ? -cre[k] : cre[k], wi = neg ? -cim[k] : cim[k];
+                const T wr = neg ? -cre[k] : cre[k];
+                if (cim[k] == (T)0) {
+                    if (t.xl == 0) {
+                        d += wr;
+                        continue;
+                    }
+                    const cx<T> a = tile[src];
+                    ar += wr * a.re;
+                    ai += wr * a.im;
+                    continue;
+                }
+                const T wi = neg ? -cim[k] : cim[k];
                 const cx<T> a = tile[src];
                 ar += wr * a.re - wi * a.im;
                 ai += wr * a.im + wi * a.re;
+            }
+            {
+                const cx<T> a = tile[u];
+                ar += d * a.re;
+                ai += d * a.im;
             }
             const uint64_t gidx = base + chunk_off[u >> l] + (u & lowmask);
             if (!p.init) {
@@ -493,14 +513,18 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     }
 }
 
-// grads[gate_of_slot[s]] = sum over blocks of partials[b][s] (fixed order).
+// grads[gate_of_slot[s]] = sum over blocks of partials[b][s]: one warp per
+// slot, lane l sums blocks l, l+32, ..., then a fixed butterfly (the order is
+// the same in every run).
 __global__ void k_sum_slots(const double *partials, uint32_t nblocks, uint32_t nslots, const uint32_t *gate_of_slot,
                             double *grads) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nslots) return;
+    const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (s >= nslots) return;  // the whole warp leaves together
     double t = 0.0;
-    for (uint32_t b = 0; b < nblocks; b++) t += partials[(size_t)b * nslots + s];
-    grads[gate_of_slot[s]] = t;
+    for (uint32_t b = lane; b < nblocks; b += 32) t += partials[(size_t)b * nslots + s];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) grads[gate_of_slot[s]] = t;
 }
 
 // ---- host orchestration ----------------------------------------------------------------
@@ -606,8 +630,8 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
         }
         if (e != cudaSuccess) return e;
         if (nslots) {
-            k_sum_slots<<<(nslots + 127) / 128, 128, 0, s.stream>>>(bufs.partials, (uint32_t)grid, nslots,
-                                                                    bufs.meta + kMaxSweepGates, bufs.grads);
+            k_sum_slots<<<(nslots + 3) / 4, 128, 0, s.stream>>>(bufs.partials, (uint32_t)grid, nslots,
+                                                                bufs.meta + kMaxSweepGates, bufs.grads);
             count_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -776,13 +800,17 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
     for (size_t seg = 0; seg < S; seg++) {
         s.queue.assign(fwd.begin() + b[seg], fwd.begin() + b[seg + 1]);
         e = flush_queue(s);
-        if (e == cudaSuccess) e = ensure_binary64(s);  // checkpoints and the reverse sweeps use binary64
         if (e != cudaSuccess) return fail_cuda(e, "forward");
         if (seg + 1 < S) {
-            e = cudaMemcpyAsync(bufs.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
+            // checkpoints are binary64 (the reverse sweeps read that form); a
+            // float-float forward state stays float-float and is exported
+            e = s.ff_resident ? launch_ff_export(s.state, bufs.ckpt[seg], s.n, s.stream)
+                              : cudaMemcpyAsync(bufs.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
             if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
         }
     }
+    e = ensure_binary64(s);  // lambda and the reverse sweeps use binary64
+    if (e != cudaSuccess) return fail_cuda(e, "forward");
     // 2. lambda = H phi, E = Re<phi|lambda>
     bool tiled = false;
     e = apply_hamiltonian_tiled<T>(s, bufs.lam, H, tiled);
