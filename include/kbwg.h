@@ -275,6 +275,13 @@ int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const
                   uintptr_t n_gates, uint32_t *order, uint32_t *sweep_end, uint64_t *tile_mask,
                   uintptr_t *n_sweeps);
 
+/* kbwg_plan for a given tile size (0: the default of a handle with these
+ * arguments; else one of the compiled sizes, KBWG_EINVAL otherwise) and
+ * fusion depth (0: 256): how a handle tuned to them would execute the gates. */
+int32_t kbwg_plan_tuned(uintptr_t num_qubits, int32_t precision, uint32_t flags, uint32_t tile_qubits,
+                        uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uint32_t *order,
+                        uint32_t *sweep_end, uint64_t *tile_mask, uintptr_t *n_sweeps);
+
 /* Make `device` current for this library on the calling thread; kbwg_new
  * places new handles on the current device (0 unless selected). */
 int32_t kbwg_select_device(int32_t device);

@@ -79,6 +79,8 @@ SIGNATURES = {
     "kbwg_build_info": (_I32, [ctypes.POINTER(ctypes.POINTER(ctypes.c_uint8)), _UP]),
     "kbwg_plan": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_uint32),
                          ctypes.POINTER(ctypes.c_uint32), _U64P, _UP]),
+    "kbwg_plan_tuned": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,
+                               ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), _U64P, _UP]),
     "kbwg_last_flush_stats": (_I32, [_P, _U64P, _U64P]),
     "kbwg_wait_probe": (_I32, [_P, ctypes.c_uint32]),
     "kbwg_stream": (_I32, [_P, ctypes.POINTER(_P)]),

@@ -929,13 +929,28 @@ int32_t kbwg_build_info(const uint8_t **msg, uintptr_t *size) {
 int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
                   uintptr_t n_gates, uint32_t *order, uint32_t *sweep_end, uint64_t *tile_mask,
                   uintptr_t *n_sweeps) {
+    const bool ff = precision && (flags & KBWG_FLAG_FAST_C128);
+    const uint32_t K = ff ? TileCfgFF::K : precision ? TileCfg<double>::K : TileCfg<float>::K;
+    return kbwg_plan_tuned(num_qubits, precision, flags, K, 0, gates, n_gates, order, sweep_end, tile_mask, n_sweeps);
+}
+
+int32_t kbwg_plan_tuned(uintptr_t num_qubits, int32_t precision, uint32_t flags, uint32_t tile_qubits,
+                        uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uint32_t *order,
+                        uint32_t *sweep_end, uint64_t *tile_mask, uintptr_t *n_sweeps) {
     GUARD_BEGIN
     if (!n_sweeps || (n_gates && (!gates || !order || !sweep_end || !tile_mask)))
         return fail(KBWG_EINVAL, "null argument");
-    const bool ff = precision && (flags & KBWG_FLAG_FAST_C128);
-    const int K = ff ? TileCfgFF::K : precision ? TileCfg<double>::K : TileCfg<float>::K;
-    const int R = ff ? TileCfgFF::R : precision ? TileCfg<double>::R : TileCfg<float>::R;
-    if (num_qubits < (uintptr_t)K || num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits outside [K, 32]");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    Sim tmp;  // the geometry rules of a handle of this size, precision and flags (no device state)
+    tmp.n = (uint32_t)num_qubits;
+    tmp.prec = precision;
+    tmp.flags = flags;
+    const uint32_t K = tile_qubits ? tile_qubits : default_tile_k(tmp);
+    const int R = (int)tile_register_bits(tmp, K);
+    if (R == 0) return fail(KBWG_EINVAL, "no sweep kernel of that tile size for this arithmetic");
+    if (fusion_depth > (uint32_t)kMaxSweepGates) return fail(KBWG_EINVAL, "fusion depth must be 0..256");
+    if (num_qubits < (uintptr_t)K) return fail(KBWG_EQUBITS, "num_qubits below the tile size");
     std::vector<GateDesc> gd(n_gates);
     for (uintptr_t i = 0; i < n_gates; i++) {
         const kbwg_gate &g = gates[i];
@@ -944,8 +959,9 @@ int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const
             return fail(KBWG_EINVAL, "bad gate");
         gd[i] = make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle);
     }
-    std::vector<PlannedSweep> plan = plan_sweeps((uint32_t)num_qubits, K, R, gd.data(), gd.size(),
-                                                 (flags & KBWG_FLAG_EXACT_ORDER) != 0);
+    std::vector<PlannedSweep> plan =
+        plan_sweeps((uint32_t)num_qubits, (int)K, R, gd.data(), gd.size(), (flags & KBWG_FLAG_EXACT_ORDER) != 0,
+                    fusion_depth ? fusion_depth : (size_t)kMaxSweepGates);
     uintptr_t pos = 0;
     for (size_t k = 0; k < plan.size(); k++) {
         for (uint32_t i : plan[k].src) order[pos++] = i;

@@ -109,6 +109,8 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
 std::vector<uint32_t> tile_options(const Sim &s);
 // The same without the qubit-count filter.
 std::vector<uint32_t> compiled_tiles(const Sim &s);
+// Register bits R of the compiled geometry with 2^k-amplitude tiles (0: none).
+uint32_t tile_register_bits(const Sim &s, uint32_t k);
 uint32_t default_tile_k(const Sim &s);
 // Tile size the next flush uses (0: one kernel per gate).
 uint32_t effective_tile_k(const Sim &s);

@@ -392,6 +392,15 @@ std::vector<uint32_t> compiled_tiles(const Sim &s) {
 // A whole small state in one tile is not preferred: one CTA on one SM ran the
 // 12-qubit Grover circuit slower (2.8 ms) than two 11-qubit tiles on two SMs
 // in five times as many sweeps (1.8 ms).
+uint32_t tile_register_bits(const Sim &s, uint32_t k) {
+    const std::vector<uint32_t> ks = compiled_tiles(s);
+    bool found = false;
+    for (uint32_t x : ks) found = found || x == k;
+    if (!found) return 0;
+    if (s.flags & KBWG_FLAG_EXACT_ORDER) return (uint32_t)(s.prec ? TileCfg<double>::R : TileCfg<float>::R);
+    return k == 11 ? 3u : 4u;  // the 2^11 tiles hold 8 amplitudes per thread, the larger ones 16
+}
+
 uint32_t default_tile_k(const Sim &s) {
     const std::vector<uint32_t> ks = compiled_tiles(s);
     if (ks[0] <= s.n) return ks[0];

@@ -427,8 +427,10 @@ def _ham_arrays(hamiltonian):
     return pa, qa, oa, ca, len(coefs)
 
 
-def plan(num_qubits, circuit, prec="c128", exact_order=False):
-    """Host planner diagnostic: list of (tile_mask, [gate indices in execution order])."""
+def plan(num_qubits, circuit, prec="c128", exact_order=False, fast_c128=False, tile_qubits=None, fusion_depth=0):
+    """Host planner diagnostic: list of (tile_mask, [gate indices in execution order]).
+    tile_qubits None: the arithmetic's default tile (kbwg_plan); otherwise
+    kbwg_plan_tuned with that tile size (0: a handle's default) and depth."""
     lib = N.load()
     n = len(circuit)
     arr = _gate_array(circuit)
@@ -436,8 +438,12 @@ def plan(num_qubits, circuit, prec="c128", exact_order=False):
     ends = (ctypes.c_uint32 * max(n, 1))()
     masks = (ctypes.c_uint64 * max(n, 1))()
     ns = ctypes.c_size_t()
-    flags = N.FLAG_EXACT_ORDER if exact_order else 0
-    N.check(lib.kbwg_plan(int(num_qubits), _DT[prec][0], flags, arr, n, order, ends, masks, ctypes.byref(ns)))
+    flags = _flags(fast_c128, exact_order)
+    if tile_qubits is None:
+        N.check(lib.kbwg_plan(int(num_qubits), _DT[prec][0], flags, arr, n, order, ends, masks, ctypes.byref(ns)))
+    else:
+        N.check(lib.kbwg_plan_tuned(int(num_qubits), _DT[prec][0], flags, int(tile_qubits), int(fusion_depth), arr, n,
+                                    order, ends, masks, ctypes.byref(ns)))
     out, b = [], 0
     for k in range(ns.value):
         e = ends[k]

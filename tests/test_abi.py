@@ -104,3 +104,40 @@ def test_planner_brickwork_sweep_count(lib, prec):
     ref = oracle.OracleDense(16, prec)
     ref.apply(C.brickwork(16, 6, 3))
     assert rel_err(o16.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
+
+
+@pytest.mark.parametrize("prec,fast,tiles", [("c64", False, (13, 12, 11)), ("c128", False, (12, 11)),
+                                             ("c128", True, (11, 12))])
+def test_planner_every_tile_size_and_depth(lib, prec, fast, tiles):
+    """The plans the autotuner chooses between: for every compiled tile size
+    and several fusion depths, the planned order only moves commuting gates
+    (replayed on the oracle), each sweep holds at most `depth` gates, and
+    every tile has the requested size with the low five qubits in it."""
+    n = 15
+    circ = C.random_circuit(n, 220, 17, max_controls=2)
+    ref = oracle.OracleDense(n, prec)
+    ref.apply(circ)
+    tol = 1e-12 if prec == "c128" else 1e-5
+    for K in tiles:
+        for depth in (256, 16, 1):
+            sweeps = plan(n, circ, prec, fast_c128=fast, tile_qubits=K, fusion_depth=depth)
+            order = [i for _, idx in sweeps for i in idx]
+            assert sorted(order) == list(range(len(circ)))
+            for mask, idx in sweeps:
+                assert bin(mask).count("1") == K and mask & 0b11111 == 0b11111
+                assert len(idx) <= depth
+            o = oracle.OracleDense(n, prec)
+            o.apply([circ[i] for i in order])
+            assert rel_err(o.state(), ref.state()) < tol, (K, depth)
+    assert len(plan(n, circ, prec, fast_c128=fast, tile_qubits=tiles[0], fusion_depth=1)) >= len(circ) // 2
+
+
+def test_planner_rejects_unknown_tile_sizes(lib):
+    circ = C.random_circuit(14, 20, 1)
+    for prec, fast, K in (("c64", False, 10), ("c128", False, 13), ("c128", True, 13)):
+        with pytest.raises(N.KbwgError) as ei:
+            plan(14, circ, prec, fast_c128=fast, tile_qubits=K)
+        assert ei.value.code == N.EINVAL
+    with pytest.raises(N.KbwgError) as ei:
+        plan(12, circ[:0], "c64", tile_qubits=13)
+    assert ei.value.code == N.EQUBITS
