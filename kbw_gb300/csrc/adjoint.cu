@@ -279,6 +279,26 @@ struct Grad<FFPol> {
     static __device__ __forceinline__ double wvalue(Wacc w) { return (double)w.h + (double)w.l; }
 };
 
+// Packed float-float amplitudes: the terms of FFPol on the unpacked pairs.
+template <>
+struct Grad<FF2B> {
+    using Amp = FF2B::Amp;
+    using G1 = Grad<FFPol>;
+    using Acc = G1::Acc;
+    static __device__ __forceinline__ FFPol::Amp unpack(const Amp &a) {
+        return FFPol::Amp{ff::f2{a.h.x, a.l.x}, ff::f2{a.h.y, a.l.y}};
+    }
+    static __device__ __forceinline__ Acc zero() { return G1::zero(); }
+    static __device__ __forceinline__ Acc term(int gt, bool one, const Amp &l, const Amp &p, const Amp &pp) {
+        return G1::term(gt, one, unpack(l), unpack(p), unpack(pp));
+    }
+    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return G1::add(a, b); }
+    static __device__ __forceinline__ Acc warp_sum(Acc a) { return G1::warp_sum(a); }
+    using Wacc = G1::Wacc;
+    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return G1::wadd(w, a); }
+    static __device__ __forceinline__ double wvalue(Wacc w) { return G1::wvalue(w); }
+};
+
 template <class P, int R, int B>
 __device__ __forceinline__ typename Grad<P>::Acc grad_pairs(int gt, const typename P::Amp (&ph)[1 << R],
                                                            const typename P::Amp (&la)[1 << R], uint32_t creg) {
@@ -853,7 +873,7 @@ int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::ve
         return adjoint_run<Fast<float>, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
                                                                                  grad_per_gate, max_ckpt);
     if (s.flags & KBWG_FLAG_FAST_C128)
-        return adjoint_run<FFPol, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
+        return adjoint_run<FF2B, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
                                                                              grad_per_gate, max_ckpt);
     return adjoint_run<Fast<double>, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
                                                                                 grad_per_gate, max_ckpt);

@@ -435,6 +435,21 @@ struct FF2 {
     }
 };
 
+// FF2's packed arithmetic on binary64 storage (the adjoint keeps its two
+// states and its checkpoints in binary64): amplitudes are split into
+// float-float pairs on the way in and rounded back on the way out, as FFPol
+// does, while the gate bodies run packed.
+struct FF2B : FF2 {
+    using Mem = cx<double>;
+    static __device__ __forceinline__ Amp from_mem(Mem a) {
+        const ff::f2 re = ff::from_double(a.re), im = ff::from_double(a.im);
+        return Amp{make_float2(re.h, im.h), make_float2(re.l, im.l)};
+    }
+    static __device__ __forceinline__ Mem to_mem(Amp a) {
+        return Mem{ff::to_double(ff::f2{a.h.x, a.l.x}), ff::to_double(ff::f2{a.h.y, a.l.y})};
+    }
+};
+
 // ---- per-gate register code -------------------------------------------------------
 // jm bit j: register j passes the gate's controls on register bits (from the
 // planner), so a controlled gate costs one predicate per register.
