@@ -279,6 +279,24 @@ struct Grad<FFPol> {
     static __device__ __forceinline__ double wvalue(Wacc w) { return (double)w.h + (double)w.l; }
 };
 
+// Packed complex64 amplitudes (float2 re, im): the terms of Fast<float>.
+template <>
+struct Grad<FastP> {
+    using Amp = FastP::Amp;
+    using G1 = Grad<Fast<float>>;
+    using Acc = G1::Acc;
+    static __device__ __forceinline__ cx<float> unpack(Amp a) { return cx<float>{a.x, a.y}; }
+    static __device__ __forceinline__ Acc zero() { return G1::zero(); }
+    static __device__ __forceinline__ Acc term(int gt, bool one, Amp l, Amp p, Amp pp) {
+        return G1::term(gt, one, unpack(l), unpack(p), unpack(pp));
+    }
+    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return G1::add(a, b); }
+    static __device__ __forceinline__ Acc warp_sum(Acc a) { return G1::warp_sum(a); }
+    using Wacc = G1::Wacc;
+    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return G1::wadd(w, a); }
+    static __device__ __forceinline__ double wvalue(Wacc w) { return G1::wvalue(w); }
+};
+
 // Packed float-float amplitudes: the terms of FFPol on the unpacked pairs.
 template <>
 struct Grad<FF2B> {
@@ -870,7 +888,7 @@ int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::ve
         return KBWG_EUNSUPPORTED;
     }
     if (s.prec == 0)
-        return adjoint_run<Fast<float>, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
+        return adjoint_run<FastP, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
                                                                                  grad_per_gate, max_ckpt);
     if (s.flags & KBWG_FLAG_FAST_C128)
         return adjoint_run<FF2B, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
