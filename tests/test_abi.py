@@ -141,3 +141,29 @@ def test_planner_rejects_unknown_tile_sizes(lib):
     with pytest.raises(N.KbwgError) as ei:
         plan(12, circ[:0], "c64", tile_qubits=13)
     assert ei.value.code == N.EQUBITS
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_planner_fuzz_commutation(lib, seed):
+    """Random registers, gate mixes (diagonal-heavy, control-heavy), tile
+    sizes and depths: the planned order must reproduce the program's state on
+    the oracle (only commuting gates move) and place every gate once."""
+    rng = np.random.default_rng(1000 + seed)
+    for _ in range(3):
+        n = int(rng.integers(13, 19))
+        kinds = [C.Z, C.P, C.RZ, C.X, C.H, C.RY] if rng.random() < 0.5 else None
+        circ = C.random_circuit(n, int(rng.integers(60, 260)), int(rng.integers(0, 1 << 30)),
+                                max_controls=int(rng.integers(0, 4)), kinds=kinds)
+        prec = "c64" if rng.random() < 0.5 else "c128"
+        fast = prec == "c128" and rng.random() < 0.5
+        tiles = {("c64", False): (13, 12, 11), ("c128", False): (12, 11), ("c128", True): (11, 12)}[(prec, fast)]
+        K = int(rng.choice(tiles))
+        depth = int(rng.choice([256, 40, 7]))
+        sweeps = plan(n, circ, prec, fast_c128=fast, tile_qubits=K, fusion_depth=depth)
+        order = [i for _, idx in sweeps for i in idx]
+        assert sorted(order) == list(range(len(circ)))
+        ref = oracle.OracleDense(n, "c128")
+        ref.apply(circ)
+        o = oracle.OracleDense(n, "c128")
+        o.apply([circ[i] for i in order])
+        assert rel_err(o.state(), ref.state()) < 1e-12, (n, K, depth)
