@@ -7,7 +7,8 @@ u * scale) to explicit uniform draws.  It shares no code with the C oracle or
 the CUDA engine; it only shares the workload generators in
 kbw_gb300/circuits.py.
 
-    python tests/golden/make_golden.py      # rewrites *.npz here
+    python tests/golden/make_golden.py          # rewrites *.npz here
+    python tests/golden/make_golden.py OUTDIR   # writes them elsewhere
 """
 import math
 import os
@@ -136,7 +137,7 @@ def encode(gates):
     return kinds, targets, masks, angles
 
 
-def main():
+def main(out=HERE):
     # 1. random small circuits with every gate kind and random controls
     cases = [(1, 30, 11), (2, 40, 12), (3, 60, 13), (5, 80, 14), (7, 100, 15), (9, 120, 16)]
     blob = {}
@@ -148,7 +149,7 @@ def main():
         blob["c%d_ctrl" % i], blob["c%d_angle" % i] = m, a
         blob["c%d_state" % i] = run(n, g)
     blob["count"] = np.int64(len(cases))
-    np.savez_compressed(os.path.join(HERE, "random_small.npz"), **blob)
+    np.savez_compressed(os.path.join(out, "random_small.npz"), **blob)
 
     # 2. Grover 12q: full probability vector for seeds 0..2, P(marked) for 0..9,
     #    and a 1024-shot histogram from seeded draws for seed 0.
@@ -167,7 +168,7 @@ def main():
             blob["sample_draws"] = draws
     blob["marked"] = np.array([x[0] for x in pm], np.int64)
     blob["p_marked"] = np.array([x[1] for x in pm], np.float64)
-    np.savez_compressed(os.path.join(HERE, "grover12.npz"), **blob)
+    np.savez_compressed(os.path.join(out, "grover12.npz"), **blob)
 
     # 3. measurement with injected draws on random entangled states
     blob = {}
@@ -189,7 +190,7 @@ def main():
         st, ct = sample(psi, qubits, 256, sd)
         blob["m%d_sdraws" % i], blob["m%d_sstates" % i], blob["m%d_scounts" % i] = sd, st, ct
     blob["count"] = np.int64(3)
-    np.savez_compressed(os.path.join(HERE, "measure.npz"), **blob)
+    np.savez_compressed(os.path.join(out, "measure.npz"), **blob)
 
     # 4. TFIM ring expectation after HEA circuits (and a Y-containing string set)
     blob = {}
@@ -203,9 +204,9 @@ def main():
                  (0.25, [(C.PAULI_Z, 2), (C.PAULI_Y, 3), (C.PAULI_X, 0)]), (2.0, [])]
         blob["e%d_mixed" % i] = np.float64(expectation(psi, n, ham_y))
     blob["count"] = np.int64(4)
-    np.savez_compressed(os.path.join(HERE, "expval.npz"), **blob)
-    print("golden fixtures written to", HERE)
+    np.savez_compressed(os.path.join(out, "expval.npz"), **blob)
+    print("golden fixtures written to", out)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)

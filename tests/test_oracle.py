@@ -1,6 +1,9 @@
 """Pins the CPU oracle (restated kbw Dense<F>) against the golden fixtures made
 by the independent numpy model and against closed-form known answers."""
 import math
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -130,3 +133,18 @@ def test_weighted_index_rule():
 def test_too_many_qubits_rejected():
     with pytest.raises(ValueError):
         oracle.OracleDense(33, "c64")
+
+
+def test_golden_fixtures_regenerate(tmp_path):
+    """The committed fixtures are exactly what tests/golden/make_golden.py
+    (the independent numpy model) produces."""
+    from conftest import GOLDEN
+    r = subprocess.run([sys.executable, os.path.join(GOLDEN, "make_golden.py"), str(tmp_path)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    for f in ("random_small.npz", "grover12.npz", "measure.npz", "expval.npz"):
+        a = np.load(os.path.join(GOLDEN, f))
+        b = np.load(os.path.join(str(tmp_path), f))
+        assert set(a.files) == set(b.files), f
+        for k in a.files:
+            assert np.allclose(a[k], b[k], rtol=0, atol=1e-13), (f, k)
