@@ -66,26 +66,30 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                                       bool keep_order, size_t max_gates) {
     max_gates = std::min(std::max<size_t>(max_gates, 1), (size_t)kMaxSweepGates);
     std::vector<PlannedSweep> out;
-    std::vector<size_t> remaining(count);
-    for (size_t i = 0; i < count; i++) remaining[i] = i;
+    // rem[start..] are the gates not placed yet, in program order; a sweep
+    // rewrites only the part of it its selection examined
+    std::vector<size_t> rem(count);
+    for (size_t i = 0; i < count; i++) rem[i] = i;
+    size_t start = 0;
     const size_t window = 8192;  // gates examined per sweep
     const int max_high = K - kLaneBits;
     // Greedy selection of a sweep's gates.  grow: the admissible high targets
     // (bits >= 5) are collected first come, first served up to max_high;
     // otherwise they are the fixed set `needed`.
     const uint64_t all_qubits = (n >= 64) ? ~0ull : ((1ull << n) - 1);
-    auto select = [&](uint64_t needed, bool grow, std::vector<size_t> *take, std::vector<size_t> *rest) {
+    // rest receives the examined gates not taken; *stop is where the
+    // examination ended (rem[*stop..] were not looked at)
+    auto select = [&](uint64_t needed, bool grow, std::vector<size_t> *take, std::vector<size_t> *rest,
+                      size_t *stop) {
         Deferred blocked;
         size_t taken = 0;
-        size_t scan = std::min(remaining.size(), window);
-        for (size_t ii = 0; ii < scan; ii++) {
-            // every qubit is a deferred non-diagonal target: no later gate can pass
-            if ((blocked.ndt & all_qubits) == all_qubits || blocked.all || taken >= max_gates) {
-                if (rest)
-                    for (size_t jj = ii; jj < scan; jj++) rest->push_back(remaining[jj]);
-                break;
-            }
-            const size_t i = remaining[ii];
+        const size_t scan = std::min(rem.size(), start + window);
+        size_t ii = start;
+        for (; ii < scan; ii++) {
+            // every qubit is a deferred non-diagonal target: no later gate can
+            // pass; or the sweep is full
+            if ((blocked.ndt & all_qubits) == all_qubits || blocked.all || taken >= max_gates) break;
+            const size_t i = rem[ii];
             const GateDesc &x = g[i];
             bool ok = blocked.passes(x) && taken < max_gates;
             if (ok && !is_diagonal(x.kind) && x.target >= (uint32_t)kLaneBits) {
@@ -105,19 +109,18 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
                 blocked.add(x, keep_order);
             }
         }
-        if (rest)
-            for (size_t ii = scan; ii < remaining.size(); ii++) rest->push_back(remaining[ii]);
+        if (stop) *stop = ii;
         return std::make_pair(taken, needed);
     };
-    while (!remaining.empty()) {
+    while (start < rem.size()) {
         // 1. choose the sweep's gates: first-come high targets, or the window
         // of max_high consecutive qubits that admits the most gates
-        auto best = select(0, true, nullptr, nullptr);
+        auto best = select(0, true, nullptr, nullptr, nullptr);
         bool best_grow = true;
         if (!keep_order && n > (uint32_t)K) {
             for (uint32_t a = kLaneBits; a + max_high <= n; a++) {
                 const uint64_t w = ((1ull << max_high) - 1) << a;
-                const auto c = select(w, false, nullptr, nullptr);
+                const auto c = select(w, false, nullptr, nullptr, nullptr);
                 if (c.first > best.first) {
                     best = c;
                     best_grow = false;
@@ -125,7 +128,8 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
             }
         }
         std::vector<size_t> take, rest;
-        const uint64_t needed = select(best_grow ? 0 : best.second, best_grow, &take, &rest).second;
+        size_t stop = start;
+        const uint64_t needed = select(best_grow ? 0 : best.second, best_grow, &take, &rest, &stop).second;
 
         PlannedSweep sw;
         choose_tile(n, K, needed, sw);
@@ -216,12 +220,14 @@ std::vector<PlannedSweep> plan_sweeps(uint32_t n, int K, int R, const GateDesc *
             pending.swap(later);
             layout ^= 1;
         }
-        // gates that did not fit go back in front, in program order
+        // gates that did not fit go back in front, in program order, ahead of
+        // the ones the selection did not examine (all later in the program)
         std::sort(leftover.begin(), leftover.end());
-        std::vector<size_t> next;
-        next.reserve(leftover.size() + rest.size());
-        std::merge(leftover.begin(), leftover.end(), rest.begin(), rest.end(), std::back_inserter(next));
-        remaining.swap(next);
+        std::vector<size_t> merged;
+        merged.reserve(leftover.size() + rest.size());
+        std::merge(leftover.begin(), leftover.end(), rest.begin(), rest.end(), std::back_inserter(merged));
+        start = stop - merged.size();  // every examined gate was taken or left in rest
+        std::copy(merged.begin(), merged.end(), rem.begin() + (std::ptrdiff_t)start);
         if (sw.gates.empty()) break;  // no gate placeable (invalid tile geometry): the caller sees the shortfall
         out.push_back(std::move(sw));
     }
