@@ -377,6 +377,51 @@ int32_t kbwg_get_tuning(kbwg_sim *sim, kbwg_tuning *out);
 int32_t kbwg_autotune(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates, uint32_t reps,
                       kbwg_tuning *out);
 
+/* ---- run-time specialised sweeps (no counterpart in the reference) ------- */
+
+/* A fused sweep normally runs one compiled kernel that interprets the
+ * sweep's gate program per tile.  A specialised kernel instead has the
+ * sweep's gates as straight-line code, every structural property (gate
+ * class, target, controls) fixed at compile time and only the angles read at
+ * run time; it is written from the plan and compiled for sm_103a with NVRTC
+ * (opened at run time) the first time a structure needs it, and cached for
+ * the process.  Modes:
+ *   KBWG_JIT_OFF    interpreted kernels only;
+ *   KBWG_JIT_AUTO   (default) a gate structure flushed before on a handle
+ *                   (from its second flush, the one that also builds its
+ *                   CUDA graph) gets specialised kernels when the state has at
+ *                   least KBWG_JIT_MIN_QUBITS (default 20) qubits;
+ *   KBWG_JIT_ALWAYS every fused flush, any size.
+ * The environment variable KBWG_JIT (0, 1, 2) sets the mode of new handles.
+ * Where NVRTC is missing or a compilation fails, the sweep runs the
+ * interpreted kernel and kbwg_jit_info reports the failure. */
+enum { KBWG_JIT_OFF = 0, KBWG_JIT_AUTO = 1, KBWG_JIT_ALWAYS = 2 };
+int32_t kbwg_set_jit(kbwg_sim *sim, int32_t mode);
+
+typedef struct kbwg_jit_stats {
+    int32_t mode;                /* the handle's KBWG_JIT_* mode */
+    int32_t available;           /* 1 if NVRTC could be opened */
+    uint64_t last_specialised;   /* sweeps of the handle's last flush that ran a specialised kernel */
+    uint64_t compiled;           /* kernels compiled in this process */
+    uint64_t reused;             /* requests served from the process's cache */
+    uint64_t failed;             /* failed compilations or loads */
+    double compile_seconds;      /* wall time spent compiling */
+} kbwg_jit_stats;
+/* sim may be NULL (then mode and last_specialised are 0).  The text of the
+ * last compilation failure is in kbwg_jit_last_error(). */
+int32_t kbwg_jit_info(kbwg_sim *sim, kbwg_jit_stats *out);
+const char *kbwg_jit_last_error(void);
+
+/* Host-only check (no GPU needed): plan `gates` as a flush on a handle with
+ * these arguments and settings would (tile_qubits / fusion_depth as for
+ * kbwg_plan_tuned) and compile the specialised kernel of every sweep with
+ * NVRTC, without loading it.  *n_sweeps: the sweeps; *n_failed: the failed
+ * compilations (text in kbwg_jit_last_error).  KBWG_EUNSUPPORTED when NVRTC
+ * is missing. */
+int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, uint32_t tile_qubits,
+                       uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uintptr_t *n_sweeps,
+                       uintptr_t *n_failed);
+
 /* ---- allocation-free entry (no counterpart in the reference) ------------- */
 
 /* For callers that cannot allocate device memory: code recorded into a CUDA

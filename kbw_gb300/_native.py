@@ -38,6 +38,14 @@ class Tuning(ctypes.Structure):
 
 TUNE_SOURCES = ("default", "set", "env", "timed", "cached")
 
+JIT_OFF, JIT_AUTO, JIT_ALWAYS = 0, 1, 2
+
+
+class JitStats(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("available", ctypes.c_int32), ("last_specialised", ctypes.c_uint64),
+                ("compiled", ctypes.c_uint64), ("reused", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("compile_seconds", ctypes.c_double)]
+
 # name -> (restype, argtypes); every function declared in include/kbwg.h
 _P = ctypes.c_void_p
 _U = ctypes.c_size_t  # uintptr_t
@@ -101,6 +109,11 @@ SIGNATURES = {
     "kbwg_set_tuning": (_I32, [_P, ctypes.c_uint32, ctypes.c_uint32]),
     "kbwg_get_tuning": (_I32, [_P, ctypes.c_void_p]),
     "kbwg_autotune": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.c_uint32, ctypes.c_void_p]),
+    "kbwg_set_jit": (_I32, [_P, _I32]),
+    "kbwg_jit_info": (_I32, [_P, ctypes.c_void_p]),
+    "kbwg_jit_last_error": (ctypes.c_char_p, []),
+    "kbwg_jit_check": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,
+                              _UP, _UP]),
     "kbwg_masked_norm_noalloc": (_I32, [_P, _U, _I32, ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "kbwg_last_error": (ctypes.c_char_p, []),
     "kbwg_launch_count": (ctypes.c_uint64, []),
@@ -147,6 +160,28 @@ def transfer_bytes():
     d2h = ctypes.c_uint64()
     check(load().kbwg_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h)))
     return int(h2d.value), int(d2h.value)
+
+
+def jit_info(handle=None):
+    """Process-wide statistics of the run-time specialised sweep kernels (and
+    the handle's mode and last flush, given a raw handle)."""
+    st = JitStats()
+    check(load().kbwg_jit_info(handle, ctypes.byref(st)))
+    return {f: getattr(st, f) for f, _ in JitStats._fields_}
+
+
+def jit_last_error():
+    return load().kbwg_jit_last_error().decode(errors="replace")
+
+
+def jit_check(num_qubits, prec, flags, gates, tile_qubits=0, fusion_depth=0):
+    """Compile (NVRTC, no GPU) the specialised kernel of every sweep a flush
+    of `gates` (a ctypes Gate array) would run; returns (sweeps, failed)."""
+    ns = ctypes.c_size_t()
+    nf = ctypes.c_size_t()
+    check(load().kbwg_jit_check(int(num_qubits), prec, int(flags), int(tile_qubits), int(fusion_depth), gates,
+                                len(gates), ctypes.byref(ns), ctypes.byref(nf)))
+    return int(ns.value), int(nf.value)
 
 
 def build_info():

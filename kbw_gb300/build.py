@@ -38,13 +38,43 @@ def headers():
     return hs + [os.path.join(ROOT, "include", "kbwg.h")]
 
 
+# Device headers compiled again at run time by NVRTC (csrc/jit.cpp): embedded
+# in the library as string literals so that it needs no source tree.
+JIT_HEADERS = ["common.cuh", "sweep.h", "ff.cuh", "ff2.cuh", "sweep_dev.cuh", "jit_dev.cuh"]
+JIT_INC = os.path.join(OBJ, "jit_sources.inc")
+
+
+def write_jit_sources():
+    """Write _build/jit_sources.inc (only when its content changes)."""
+    delim = "KBWGJIT"
+    names, bodies = [], []
+    for h in JIT_HEADERS:
+        with open(os.path.join(CSRC, h)) as f:
+            text = f.read()
+        if ")" + delim + '"' in text:
+            raise RuntimeError("%s contains the raw-string delimiter" % h)
+        names.append('"%s"' % h)
+        bodies.append('R"%s(%s)%s"' % (delim, text, delim))
+    out = ("// Generated by kbw_gb300/build.py from csrc/: device headers for NVRTC.\n"
+           "static const char *const kJitHeaderNames[] = {%s};\n"
+           "static const char *const kJitHeaderSources[] = {\n%s};\n"
+           "static const int kJitHeaderCount = %d;\n") % (", ".join(names), ",\n".join(bodies), len(names))
+    old = None
+    if os.path.exists(JIT_INC):
+        with open(JIT_INC) as f:
+            old = f.read()
+    if old != out:
+        with open(JIT_INC, "w") as f:
+            f.write(out)
+
+
 def _compile(src, verbose):
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-    newest_dep = max(os.path.getmtime(p) for p in headers() + [src, __file__])
+    newest_dep = max(os.path.getmtime(p) for p in headers() + [src, __file__, JIT_INC])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, ""
     cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-           "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")] + ARCH
+           "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", OBJ] + ARCH
     if src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"] if verbose else []
     cmd += ["-c", src, "-o", obj]
@@ -60,6 +90,7 @@ def build(verbose=False, force=False):
     if force:
         for f in os.listdir(OBJ):
             os.remove(os.path.join(OBJ, f))
+    write_jit_sources()
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(s, verbose), srcs))

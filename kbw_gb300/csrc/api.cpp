@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/kbwg.h"
+#include "jit.h"
 #include "sim.h"
 #include "sweep.h"
 #include "tune.h"
@@ -107,6 +108,7 @@ static cudaError_t flush_t(Sim &s) {
     if (s.queue.empty()) return cudaSuccess;
     cudaError_t e = cudaSuccess;
     s.last_gates = s.queue.size();
+    s.last_specialised = 0;
     if (s.flags & KBWG_FLAG_NO_FUSION) {
         for (const GateDesc &g : s.queue) {
             if (s.prof.on) s.prof.mark(s.stream);
@@ -268,6 +270,7 @@ int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_s
     char *end = nullptr;
     unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
     s->rng = (seed && end && *end == 0 && *seed) ? (uint64_t)sv : (uint64_t)(uintptr_t)s ^ 0x5DEECE66Dull;
+    s->jit_mode = jit_default_mode();
     std::string tmsg;
     const int32_t trc = apply_env_tuning(*s, tmsg);
     if (trc != KBWG_OK) return cleanup(trc, tmsg);
@@ -973,6 +976,41 @@ int32_t kbwg_plan_tuned(uintptr_t num_qubits, int32_t precision, uint32_t flags,
     GUARD_END
 }
 
+int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, uint32_t tile_qubits,
+                       uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uintptr_t *n_sweeps,
+                       uintptr_t *n_failed) {
+    GUARD_BEGIN
+    if (!n_sweeps || !n_failed || (n_gates && !gates)) return fail(KBWG_EINVAL, "null argument");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    if (!jit_available()) return fail(KBWG_EUNSUPPORTED, "NVRTC (libnvrtc.so.13) not found");
+    Sim tmp;  // the rules of a handle of this size, precision and flags (no device state)
+    tmp.n = (uint32_t)num_qubits;
+    tmp.prec = precision;
+    tmp.flags = flags;
+    if (tile_qubits) {
+        const std::vector<uint32_t> ks = tile_options(tmp);
+        if (std::find(ks.begin(), ks.end(), tile_qubits) == ks.end())
+            return fail(KBWG_EINVAL, "no sweep kernel of that tile size for this arithmetic");
+    }
+    if (fusion_depth > (uint32_t)kMaxSweepGates) return fail(KBWG_EINVAL, "fusion depth must be 0..256");
+    tmp.tile_k = tile_qubits;
+    tmp.fusion_depth = fusion_depth;
+    std::vector<GateDesc> gd(n_gates);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ || g.target >= num_qubits || (g.control_mask >> num_qubits) ||
+            (g.control_mask & (1ull << g.target)))
+            return fail(KBWG_EINVAL, "bad gate");
+        gd[i] = make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle);
+    }
+    size_t sweeps = 0;
+    *n_failed = jit_check(tmp, gd.data(), gd.size(), sweeps);
+    *n_sweeps = sweeps;
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_select_device(int32_t device) {
     CUDA_TRY(cudaSetDevice(device));
     return KBWG_OK;
@@ -1319,6 +1357,34 @@ int32_t kbwg_autotune(kbwg_sim *s, const kbwg_gate *gates, uintptr_t n_gates, ui
     if (out) fill_tuning(*s, out);
     return KBWG_OK;
     GUARD_END
+}
+
+int32_t kbwg_set_jit(kbwg_sim *s, int32_t mode) {
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    if (mode < KBWG_JIT_OFF || mode > KBWG_JIT_ALWAYS) return fail(KBWG_EINVAL, "bad JIT mode");
+    s->jit_mode = mode;
+    return KBWG_OK;
+}
+
+int32_t kbwg_jit_info(kbwg_sim *s, kbwg_jit_stats *out) {
+    GUARD_BEGIN
+    if (!out) return fail(KBWG_EINVAL, "null argument");
+    const JitStats st = jit_stats();
+    out->mode = s ? s->jit_mode : 0;
+    out->available = jit_available() ? 1 : 0;
+    out->last_specialised = s ? s->last_specialised : 0;
+    out->compiled = st.compiled;
+    out->reused = st.reused;
+    out->failed = st.failed;
+    out->compile_seconds = st.compile_s;
+    return KBWG_OK;
+    GUARD_END
+}
+
+const char *kbwg_jit_last_error(void) {
+    static thread_local std::string msg;
+    msg = jit_last_error();
+    return msg.c_str();
 }
 
 const char *kbwg_last_error(void) { return g_last_error.c_str(); }

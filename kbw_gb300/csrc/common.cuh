@@ -1,14 +1,19 @@
 // Shared device/host definitions of the GB300 dense state-vector engine.
 #pragma once
 
-#include <cuda_runtime.h>
 #include <stdint.h>
+
+// Host-only parts are left out when NVRTC compiles the run-time-generated
+// sweep kernels (jit.cpp), which see only the device definitions.
+#if !defined(__CUDACC_RTC__)
+#include <cuda_runtime.h>
 
 #include <atomic>
 #include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
+#endif
 
 namespace kbwg {
 
@@ -19,6 +24,7 @@ struct alignas(2 * sizeof(T)) cx {
     T re, im;
 };
 
+#if !defined(__CUDACC_RTC__)
 // Kernel launch counter (all handles, this process).
 extern std::atomic<uint64_t> g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -54,6 +60,8 @@ inline cudaError_t current_sm_count(int &sms) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return e;
 }
+
+#endif  // !__CUDACC_RTC__
 
 // One gate as the kernels see it.  Constants are pre-computed on the host in
 // the state precision F exactly as the reference does (cos/sin of F(theta/2),
@@ -198,6 +206,7 @@ __host__ __device__ __forceinline__ bool touches_only_one(uint32_t kind) {
     return kind == G_Z || kind == G_P;
 }
 
+#if !defined(__CUDACC_RTC__)
 // ---- host-side error plumbing ----------------------------------------------
 struct Status {
     int32_t code = 0;
@@ -205,5 +214,6 @@ struct Status {
 };
 
 void set_error(int32_t code, const std::string &msg);
+#endif  // !__CUDACC_RTC__
 
 }  // namespace kbwg

@@ -18,7 +18,9 @@
 #pragma once
 
 #include <stdint.h>
+#if !defined(__CUDACC_RTC__)
 #include <string.h>
+#endif
 
 #if defined(__CUDACC__)
 #define FFI __host__ __device__ __forceinline__

@@ -78,8 +78,12 @@ struct Sim {
     uint32_t tune_source = 0, tune_candidates = 0;
     double tune_ms = 0.0, tune_default_ms = 0.0;
 
+    // run-time specialised sweep kernels: KBWG_JIT_OFF / _AUTO / _ALWAYS
+    int jit_mode = 1;
+
     // statistics of the last flush
     uint64_t last_passes = 0;
+    uint64_t last_specialised = 0;  // sweeps of it that ran a specialised kernel
     uint64_t last_gates = 0;
 };
 
@@ -102,6 +106,11 @@ cudaError_t flush_queue(Sim &s);
 
 // Fusion planner entry used by flush_queue (sweep.cu).
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
+
+// Write and compile (NVRTC, without loading: no GPU needed) the specialised
+// kernel of every sweep a flush of `gates` would run on `s`; returns the
+// number of failed compilations and sets `sweeps`.
+size_t jit_check(const Sim &s, const GateDesc *gates, size_t count, size_t &sweeps);
 
 // Tile sizes K (2^K amplitudes per tile) with a compiled sweep kernel for
 // the handle's arithmetic and qubit count, the default first; empty when the

@@ -29,11 +29,20 @@
 #include <math.h>
 
 #include "../../include/kbwg.h"
+#include "jit.h"
 #include "kernels.h"
 #include "sim.h"
 #include "sweep_dev.cuh"
 
 namespace kbwg {
+
+// C++ names of the arithmetic policies, for the run-time specialised kernels.
+template <class P> struct PolicyName;
+template <> struct PolicyName<Exact<float>> { static constexpr const char *s = "kbwg::Exact<float>"; };
+template <> struct PolicyName<Exact<double>> { static constexpr const char *s = "kbwg::Exact<double>"; };
+template <> struct PolicyName<Fast<double>> { static constexpr const char *s = "kbwg::Fast<double>"; };
+template <> struct PolicyName<FastP> { static constexpr const char *s = "kbwg::FastP"; };
+template <> struct PolicyName<FF2> { static constexpr const char *s = "kbwg::FF2"; };
 
 template <class P, int K, int R>
 struct SweepKernel {
@@ -173,6 +182,7 @@ cudaError_t launch_wait_probe(int *err, uint32_t spins, cudaStream_t s) {
 // planner and the per-launch host overhead.
 struct SweepGraph {
     const void *kernel = nullptr;   // which k_sweep instantiation
+    size_t specialised = 0;         // sweeps that run a run-time specialised kernel
     std::vector<uint64_t> sig;      // structure of the flushed gate list
     std::vector<uint32_t> src;      // program slot -> index in the flushed list
     std::vector<TileGate> planned;  // program with unpacked constants
@@ -212,10 +222,13 @@ static uint64_t hash_of(const std::vector<uint64_t> &sig) {
     return h;
 }
 
+// Kind, target and controls of every gate; for the float-float path's
+// |1> * i^q gates also q, which the specialised kernels compile in.
 static std::vector<uint64_t> structure_of(const GateDesc *gates, size_t count) {
     std::vector<uint64_t> sig(2 * count);
     for (size_t i = 0; i < count; i++) {
         sig[2 * i] = (uint64_t)gates[i].kind | ((uint64_t)gates[i].target << 8);
+        if (gates[i].kind == G_PI) sig[2 * i] |= (uint64_t)(int)gates[i].c[0] << 40;
         sig[2 * i + 1] = gates[i].ctrl;
     }
     return sig;
@@ -247,34 +260,36 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     const void *kid = (const void *)k_sweep<P, K, R>;
     const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
     // timed profiling marks every launch with events, which a graph replay cannot
-    bool graphs = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
+    const bool graphs_ok = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
+    bool repeat = false;  // this gate structure was flushed before on the handle
     std::vector<uint64_t> sig;
-    if (graphs) {
+    if (graphs_ok || s.jit_mode == KBWG_JIT_AUTO) {
         if (!s.graphs) s.graphs = new GraphCache();
         GraphCache &gc = *(GraphCache *)s.graphs;
         sig = structure_of(gates, count);
         sig.push_back((uint64_t)(uintptr_t)kid);
         sig.push_back(depth);
         const uint64_t h = hash_of(sig);
-        bool again = false;
-        for (uint64_t x : gc.seen) again = again || x == h;
-        if (!again) {  // first sight of this structure: launch directly, remember it
+        for (uint64_t x : gc.seen) repeat = repeat || x == h;
+        if (!repeat) {  // first sight of this structure: launch directly, remember it
             if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
             gc.seen.push_back(h);
-            graphs = false;
         }
-        for (SweepGraph &g : gc.entries) {
-            if (g.kernel != kid || g.sig != sig) continue;
-            cudaError_t e = upload_program<P>(s, g.planned, g.src, gates, g.dprog);
-            if (e != cudaSuccess) return e;
-            e = cudaGraphLaunch(g.exec, s.stream);
-            if (e != cudaSuccess) return e;
-            for (size_t i = 0; i < g.sweeps; i++) count_launch();
-            g.last_use = ++gc.clock;
-            s.last_passes = g.sweeps;
-            return cudaSuccess;
-        }
+        if (graphs_ok)
+            for (SweepGraph &g : gc.entries) {
+                if (g.kernel != kid || g.sig != sig) continue;
+                cudaError_t e = upload_program<P>(s, g.planned, g.src, gates, g.dprog);
+                if (e != cudaSuccess) return e;
+                e = cudaGraphLaunch(g.exec, s.stream);
+                if (e != cudaSuccess) return e;
+                for (size_t i = 0; i < g.sweeps; i++) count_launch();
+                g.last_use = ++gc.clock;
+                s.last_passes = g.sweeps;
+                s.last_specialised = g.specialised;
+                return cudaSuccess;
+            }
     }
+    const bool graphs = graphs_ok && repeat;  // a graph is built on the second sight
     std::vector<PlannedSweep> plan =
         plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0, depth);
     std::vector<TileGate> planned;
@@ -303,6 +318,24 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     const TileGate *dprog = (const TileGate *)dbuf;
     const uint64_t tiles = 1ull << (s.n - K);
     const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * SK::kCtasPerSm);
+    // Run-time specialised kernels (jit.cpp): for a structure flushed before
+    // on a large enough state (from its second flush, which also builds its
+    // graph), or on every flush in KBWG_JIT_ALWAYS mode.  A sweep whose kernel
+    // could not be built runs the interpreted k_sweep.
+    std::vector<const void *> jk;
+    if (s.jit_mode == KBWG_JIT_ALWAYS || (s.jit_mode == KBWG_JIT_AUTO && repeat && s.n >= jit_min_qubits())) {
+        const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+        jit_sweep_kernels(geo, plan, jk);
+        for (const void *f : jk) {
+            if (!f) continue;
+            e = ensure_smem_limit(f, SK::kSmem);
+            if (e != cudaSuccess) {
+                if (graphs) cudaFree(dbuf);
+                return e;
+            }
+        }
+    }
+    size_t specialised = 0;
     if (graphs) {
         e = cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) {
@@ -329,7 +362,15 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         p.tiles = tiles;
         off += sw.gates.size();
         if (s.prof.on) s.prof.mark(s.stream);
-        k_sweep<P, K, R><<<(unsigned)grid, SK::kThreads, SK::kSmem, s.stream>>>((Mem *)s.state, p);
+        const void *spec = jk.empty() ? nullptr : jk[(size_t)(&sw - plan.data())];
+        if (spec) {
+            Mem *stp = (Mem *)s.state;
+            void *args[] = {(void *)&stp, (void *)&p};
+            cudaLaunchKernel(spec, dim3((unsigned)grid), dim3(SK::kThreads), args, SK::kSmem, s.stream);
+            specialised++;
+        } else {
+            k_sweep<P, K, R><<<(unsigned)grid, SK::kThreads, SK::kSmem, s.stream>>>((Mem *)s.state, p);
+        }
         if (!graphs) count_launch();
         e = cudaGetLastError();
         if (s.prof.on) {
@@ -339,6 +380,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         if (e != cudaSuccess) break;
     }
     s.last_passes = plan.size();
+    s.last_specialised = specialised;
     if (!graphs) return e;
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(s.stream, &graph);
@@ -365,6 +407,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     }
     SweepGraph g;
     g.kernel = kid;
+    g.specialised = specialised;
     g.sig = std::move(sig);
     g.src = std::move(src);
     g.planned = std::move(planned);
@@ -546,6 +589,54 @@ cudaError_t init_state(Sim &s) {
     }
     s.ff_resident = false;
     return s.prec ? launch_init<double>(s.state, s.n, s.stream) : launch_init<float>(s.state, s.n, s.stream);
+}
+
+// ---- compile-only check of the specialised kernels (no GPU) --------------------
+template <class P, int K, int R>
+static size_t check_p(const Sim &s, const GateDesc *gates, size_t count, size_t &sweeps) {
+    using SK = SweepKernel<P, K, R>;
+    const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
+    const std::vector<PlannedSweep> plan =
+        plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0, depth);
+    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+    std::vector<std::string> srcs;
+    for (const PlannedSweep &sw : plan) srcs.push_back(jit_sweep_source(geo, sw));
+    sweeps = plan.size();
+    return jit_compile_only(srcs);
+}
+
+template <class T>
+static size_t check_t(const Sim &s, const GateDesc *gates, size_t count, size_t &sweeps) {
+    constexpr int K = TileCfg<T>::K, R = TileCfg<T>::R;
+    const uint32_t tk = chosen_tile(s);
+    if (tk != (uint32_t)K && !(s.flags & KBWG_FLAG_EXACT_ORDER)) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (tk == 12) return check_p<FastP, 12, 4>(s, gates, count, sweeps);
+            if (tk == 11) return check_p<FastP, 11, 3>(s, gates, count, sweeps);
+        } else {
+            if (tk == 11) return check_p<Fast<T>, 11, 3>(s, gates, count, sweeps);
+        }
+    }
+    sweeps = 0;
+    if (s.n < (uint32_t)K) return 0;
+    if (s.flags & KBWG_FLAG_EXACT_ORDER) return check_p<Exact<T>, K, R>(s, gates, count, sweeps);
+    if constexpr (std::is_same<T, float>::value) return check_p<FastP, K, R>(s, gates, count, sweeps);
+    else return check_p<Fast<T>, K, R>(s, gates, count, sweeps);
+}
+
+size_t jit_check(const Sim &s, const GateDesc *gates, size_t count, size_t &sweeps) {
+    std::vector<GateDesc> folded;
+    if (!(s.flags & (KBWG_FLAG_EXACT_ORDER | KBWG_FLAG_NO_FOLD))) {
+        folded = fold_diagonals(gates, count);
+        gates = folded.data();
+        count = folded.size();
+    }
+    if (ff_capable(s)) {
+        std::vector<GateDesc> g = ff_rewrite(gates, count);
+        if (chosen_tile(s) == 12) return check_p<FF2, 12, 4>(s, g.data(), g.size(), sweeps);
+        return check_p<FF2, TileCfgFF::K, TileCfgFF::R>(s, g.data(), g.size(), sweeps);
+    }
+    return s.prec ? check_t<double>(s, gates, count, sweeps) : check_t<float>(s, gates, count, sweeps);
 }
 
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {

@@ -3,7 +3,9 @@
 
 #include <stdint.h>
 
+#if !defined(__CUDACC_RTC__)
 #include <vector>
+#endif
 
 #include "common.cuh"
 
@@ -110,6 +112,7 @@ struct SweepParams {
     uint64_t tiles;                  // 2^(n-K)
 };
 
+#if !defined(__CUDACC_RTC__)
 struct PlannedSweep {
     uint32_t l = 0, m = 0;
     uint8_t hq[16] = {0};
@@ -152,5 +155,6 @@ struct PauliPass {
 };
 std::vector<PauliPass> plan_pauli_passes(uint32_t n, int K, const std::vector<uint64_t> &xmasks, size_t max_terms,
                                          std::vector<size_t> &wide);
+#endif  // !__CUDACC_RTC__
 
 }  // namespace kbwg

@@ -4,7 +4,9 @@
 // and the per-gate register/shuffle code.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <string.h>
+#endif
 
 #include "ff.cuh"
 #include "ff2.cuh"
@@ -85,12 +87,14 @@ struct Exact {
     // Constants are stored in T on the host (exact: they are T values widened
     // to double), so no thread converts precision at run time (a
     // float<->double conversion issues at the FP64 rate on this chip).
+#if !defined(__CUDACC_RTC__)
     static void pack_host(TileGate &g) {
         T v[4];
         for (int i = 0; i < 4; i++) v[i] = (T)g.c[i];
         memset(g.c, 0, sizeof g.c);
         memcpy(g.c, v, sizeof v);
     }
+#endif
     struct K4 {
         T c0, c1, c2, c3;
     };
@@ -159,14 +163,16 @@ template <class T>
 struct Fast : Exact<T> {
     using Amp = cx<T>;
     using K4 = typename Exact<T>::K4;
+    // (the products are explicitly rounded: a plain product could be fused
+    // with the next gate's sum once gates run as straight-line code)
     static __device__ __forceinline__ void h_pair(int, const K4 &k, Amp &a0, Amp &a1) {
-        const Amp n0{(a0.re + a1.re) * k.c0, (a0.im + a1.im) * k.c0};
-        const Amp n1{(a0.re - a1.re) * k.c0, (a0.im - a1.im) * k.c0};
+        const Amp n0{xmul(a0.re + a1.re, k.c0), xmul(a0.im + a1.im, k.c0)};
+        const Amp n1{xmul(a0.re - a1.re, k.c0), xmul(a0.im - a1.im, k.c0)};
         a0 = n0;
         a1 = n1;
     }
     static __device__ __forceinline__ Amp h_half(int, const K4 &k, Amp self, Amp o, T sgn) {
-        return Amp{fma(sgn, self.re, o.re) * k.c0, fma(sgn, self.im, o.im) * k.c0};
+        return Amp{xmul(fma(sgn, self.re, o.re), k.c0), xmul(fma(sgn, self.im, o.im), k.c0)};
     }
     static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
         const Amp n0{fma(k.c0, a0.re, k.c1 * a1.im), fma(k.c0, a0.im, -k.c1 * a1.re)};
@@ -202,7 +208,9 @@ struct FastP {
     using K4 = Exact<float>::K4;
     static __device__ __forceinline__ Amp from_mem(Mem a) { return make_float2(a.re, a.im); }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return Mem{a.x, a.y}; }
+#if !defined(__CUDACC_RTC__)
     static void pack_host(TileGate &g) { Exact<float>::pack_host(g); }
+#endif
     static __device__ __forceinline__ K4 load(const TileGate &g) { return Exact<float>::load(g); }
     static __device__ __forceinline__ Amp shfl(Amp v, int m) {
         return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
@@ -218,15 +226,21 @@ struct FastP {
     static __device__ __forceinline__ Amp y_half(Amp o, bool one) {
         return one ? make_float2(-o.y, o.x) : make_float2(o.y, -o.x);
     }
+    // H is the one gate whose results are bare products.  A packed product
+    // can be fused into the next gate's packed sum once gates run as
+    // straight-line code (one rounding fewer), so it is rounded lane by lane
+    // with the scalar multiply, which is never fused.
+    static __device__ __forceinline__ float2 mul_rn(float2 a, float c) {
+        return make_float2(__fmul_rn(a.x, c), __fmul_rn(a.y, c));
+    }
     static __device__ __forceinline__ void h_pair(int, const K4 &k, Amp &a0, Amp &a1) {
-        const float2 c = bc(k.c0);
-        const Amp n0 = __fmul2_rn(__fadd2_rn(a0, a1), c);
-        const Amp n1 = __fmul2_rn(ff2::sub(a0, a1), c);
+        const Amp n0 = mul_rn(__fadd2_rn(a0, a1), k.c0);
+        const Amp n1 = mul_rn(ff2::sub(a0, a1), k.c0);
         a0 = n0;
         a1 = n1;
     }
     static __device__ __forceinline__ Amp h_half(int, const K4 &k, Amp self, Amp o, float sgn) {
-        return __fmul2_rn(__ffma2_rn(bc(sgn), self, o), bc(k.c0));
+        return mul_rn(__ffma2_rn(bc(sgn), self, o), k.c0);
     }
     static __device__ __forceinline__ void rx_pair(const K4 &k, Amp &a0, Amp &a1) {
         const float2 c = bc(k.c0), s = make_float2(k.c1, -k.c1);
@@ -275,6 +289,7 @@ struct FFPol {
         return Amp{ff::from_double(a.re), ff::from_double(a.im)};
     }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return Mem{ff::to_double(a.re), ff::to_double(a.im)}; }
+#if !defined(__CUDACC_RTC__)
     static void pack_host(TileGate &g) {
         double c[4] = {g.c[0], g.c[1], g.c[2], g.c[3]};
         float f[8];
@@ -285,6 +300,7 @@ struct FFPol {
         }
         memcpy(g.c, f, sizeof f);
     }
+#endif
     static __device__ __forceinline__ K4 load(const TileGate &g) {
         const float *f = reinterpret_cast<const float *>(g.c);
         return K4{{f[0], f[1]}, {f[2], f[3]}, {f[4], f[5]}, {f[6], f[7]}};
@@ -369,7 +385,9 @@ struct FF2 {
     using K4 = FFPol::K4;
     static __device__ __forceinline__ Amp from_mem(Mem a) { return a; }
     static __device__ __forceinline__ Mem to_mem(Amp a) { return a; }
+#if !defined(__CUDACC_RTC__)
     static void pack_host(TileGate &g) { FFPol::pack_host(g); }
+#endif
     static __device__ __forceinline__ K4 load(const TileGate &g) { return FFPol::load(g); }
     static __device__ __forceinline__ Amp shfl(Amp v, int m) {
         Amp r;

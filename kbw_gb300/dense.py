@@ -33,7 +33,7 @@ class DenseGB300:
     """One state vector of 2^n amplitudes on the current CUDA device."""
 
     def __init__(self, num_qubits, prec="c128", fusion=True, fast_c128=False, exact_order=False, graphs=True,
-                 fold=True):
+                 fold=True, jit=None):
         lib = N.load()
         if prec not in _DT:
             raise ValueError("prec must be 'c64' or 'c128'")
@@ -47,6 +47,8 @@ class DenseGB300:
         N.check(lib.kbwg_new(self.num_qubits, _DT[prec][0], flags, ctypes.byref(h)))
         self._h = h
         self._lib = lib
+        if jit is not None:
+            self.set_jit(jit)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -260,6 +262,15 @@ class DenseGB300:
         p = ctypes.c_uint64()
         N.check(self._lib.kbwg_last_flush_stats(self._h, ctypes.byref(g), ctypes.byref(p)))
         return int(g.value), int(p.value)
+
+    def set_jit(self, mode):
+        """Run-time specialised sweep kernels: N.JIT_OFF, N.JIT_AUTO or N.JIT_ALWAYS."""
+        N.check(self._lib.kbwg_set_jit(self._h, int(mode)))
+
+    def jit_info(self):
+        """The handle's JIT mode, how many sweeps of its last flush ran a
+        specialised kernel, and the process-wide compile statistics."""
+        return N.jit_info(self._h)
 
     def wait_probe(self, spins=1024):
         """Run the tile kernels' bounded wait on a barrier nothing completes;

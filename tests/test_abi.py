@@ -167,3 +167,24 @@ def test_planner_fuzz_commutation(lib, seed):
         o = oracle.OracleDense(n, "c128")
         o.apply([circ[i] for i in order])
         assert rel_err(o.state(), ref.state()) < 1e-12, (n, K, depth)
+
+
+# (precision, flags, tile size): every arithmetic's default geometry, one
+# other geometry, the order-preserving mode
+JIT_CASES = [(N.C128, N.FLAG_FAST_C128, 0), (N.C64, 0, 0), (N.C128, 0, 11), (N.C64, N.FLAG_EXACT_ORDER, 0)]
+
+
+@pytest.mark.parametrize("prec,flags,tile", JIT_CASES)
+def test_specialised_sweep_kernels_compile(lib, prec, flags, tile):
+    """Every sweep of a planned circuit gets a run-time specialised kernel
+    source that NVRTC compiles for sm_103a (host only; no GPU needed)."""
+    from kbw_gb300.dense import _gate_array
+    circ = C.random_circuit(16, 160, 21, max_controls=3)
+    try:
+        sweeps, failed = N.jit_check(16, prec, flags, _gate_array(circ), tile)
+    except N.KbwgError as e:
+        if e.code == N.EUNSUPPORTED:
+            pytest.skip("NVRTC not available: %s" % e)
+        raise
+    assert sweeps > 0
+    assert failed == 0, N.jit_last_error()
