@@ -388,15 +388,23 @@ int32_t kbwg_autotune(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates, 
  * the process.  Modes:
  *   KBWG_JIT_OFF    interpreted kernels only;
  *   KBWG_JIT_AUTO   (default) a gate structure flushed before on a handle
- *                   (from its second flush, the one that also builds its
- *                   CUDA graph) gets specialised kernels when the state has at
- *                   least KBWG_JIT_MIN_QUBITS (default 20) qubits;
- *   KBWG_JIT_ALWAYS every fused flush, any size.
+ *                   gets specialised kernels, compiled in the background,
+ *                   when the state has at least KBWG_JIT_MIN_QUBITS (default
+ *                   20) qubits;
+ *   KBWG_JIT_ALWAYS every fused flush, any size, compiling synchronously.
  * The environment variable KBWG_JIT (0, 1, 2) sets the mode of new handles.
  * Where NVRTC is missing or a compilation fails, the sweep runs the
  * interpreted kernel and kbwg_jit_info reports the failure. */
 enum { KBWG_JIT_OFF = 0, KBWG_JIT_AUTO = 1, KBWG_JIT_ALWAYS = 2 };
 int32_t kbwg_set_jit(kbwg_sim *sim, int32_t mode);
+
+/* In auto mode the specialised kernels of a structure are compiled in the
+ * background from its second flush on, while flushes keep running the
+ * interpreted kernels (the same amplitudes); the first flush after the
+ * compilation has finished takes them in.  kbwg_jit_wait blocks until the
+ * handle's pending compilations have finished, so that the next flush of
+ * each of those structures runs specialised (e.g. before a timed region). */
+int32_t kbwg_jit_wait(kbwg_sim *sim);
 
 typedef struct kbwg_jit_stats {
     int32_t mode;                /* the handle's KBWG_JIT_* mode */

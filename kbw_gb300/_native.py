@@ -110,6 +110,7 @@ SIGNATURES = {
     "kbwg_get_tuning": (_I32, [_P, ctypes.c_void_p]),
     "kbwg_autotune": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.c_uint32, ctypes.c_void_p]),
     "kbwg_set_jit": (_I32, [_P, _I32]),
+    "kbwg_jit_wait": (_I32, [_P]),
     "kbwg_jit_info": (_I32, [_P, ctypes.c_void_p]),
     "kbwg_jit_last_error": (ctypes.c_char_p, []),
     "kbwg_jit_check": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,

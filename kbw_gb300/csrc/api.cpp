@@ -1366,6 +1366,14 @@ int32_t kbwg_set_jit(kbwg_sim *s, int32_t mode) {
     return KBWG_OK;
 }
 
+int32_t kbwg_jit_wait(kbwg_sim *s) {
+    GUARD_BEGIN
+    if (!s) return fail(KBWG_EINVAL, "null handle");
+    wait_specialised(*s);
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_jit_info(kbwg_sim *s, kbwg_jit_stats *out) {
     GUARD_BEGIN
     if (!out) return fail(KBWG_EINVAL, "null argument");

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -98,7 +99,8 @@ struct Compiled {
 };
 
 std::mutex g_mu;
-std::unordered_map<std::string, Compiled> g_cache;  // full source (+ entry) -> loaded kernel
+std::unordered_map<std::string, Compiled> g_cache;     // full source (+ entry) -> loaded kernel
+std::unordered_map<std::string, std::string> g_cubins;  // source -> cubin compiled in the background
 std::string g_last_error;
 JitStats g_stats;
 
@@ -201,12 +203,12 @@ int env_int(const char *name, int dflt) {
 
 const char *kClassName[] = {"TG_X", "TG_Y", "TG_H", "TG_RX", "TG_RY", "TG_Z", "TG_P", "TG_RZ", "TG_PI", "TG_SCALE"};
 
-void run_parallel(size_t count, const std::function<void(size_t)> &fn) {
+void run_parallel(size_t count, const std::function<void(size_t)> &fn, bool on_device = true) {
     const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
     const size_t nthreads = std::min<size_t>(count, std::min<size_t>(hw, 32));
     std::atomic<size_t> next{0};
     int dev = 0;
-    const bool have_dev = cudaGetDevice(&dev) == cudaSuccess;
+    const bool have_dev = on_device && cudaGetDevice(&dev) == cudaSuccess;
     auto worker = [&]() {
         if (have_dev) cudaSetDevice(dev);  // library loads happen on the caller's device
         for (size_t w; (w = next.fetch_add(1)) < count;) fn(w);
@@ -346,16 +348,30 @@ const void *jit_kernel(const std::string &src, const char *entry) {
             return (const void *)it->second.kernel;
         }
     }
-    const auto t0 = std::chrono::steady_clock::now();
-    const std::string cubin = compile_cubin(src);
-    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::string cubin;
+    bool fresh = false;
+    double dt = 0.0;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_cubins.find(src);
+        if (it != g_cubins.end()) {
+            cubin.swap(it->second);
+            g_cubins.erase(it);
+        }
+    }
+    if (cubin.empty()) {
+        const auto t0 = std::chrono::steady_clock::now();
+        cubin = compile_cubin(src);
+        dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fresh = true;
+    }
     if (cubin.empty()) return nullptr;
     Compiled c;
     const void *k = load_kernel(cubin, entry, c);
     std::lock_guard<std::mutex> lk(g_mu);
     g_stats.compile_s += dt;
     if (!k) return nullptr;
-    g_stats.compiled++;
+    if (fresh) g_stats.compiled++;
     auto ins = g_cache.emplace(key, c);
     if (!ins.second) {  // another thread loaded the same source meanwhile: keep one
         cudaLibraryUnload(c.lib);
@@ -382,6 +398,95 @@ size_t jit_compile_only(const std::vector<std::string> &srcs) {
             failed++;
     });
     return failed.load();
+}
+
+// ---- background compilation -----------------------------------------------------
+struct JitJob {
+    std::vector<std::string> srcs;
+    std::atomic<bool> done{false};
+    std::mutex mu;
+    std::condition_variable cv;
+};
+
+namespace {
+// Worker threads of the background jobs.  Defined after the caches it fills,
+// so it is destroyed first at exit: the destructor stops the jobs between
+// compilations and joins them while the caches still exist.
+struct Runner {
+    std::mutex mu;
+    std::vector<std::pair<std::thread, std::shared_ptr<JitJob>>> threads;
+    std::atomic<bool> stop{false};
+    ~Runner() {
+        stop = true;
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto &t : threads)
+            if (t.first.joinable()) t.first.join();
+    }
+};
+Runner g_runner;
+
+void run_job(std::shared_ptr<JitJob> job) {
+    std::vector<size_t> todo;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        for (size_t i = 0; i < job->srcs.size(); i++) {
+            const std::string &src = job->srcs[i];
+            if (g_cubins.count(src) || g_cache.count(src + '\0' + "kbwg_jit_sweep")) continue;
+            bool dup = false;
+            for (size_t j : todo) dup = dup || job->srcs[j] == src;
+            if (!dup) todo.push_back(i);
+        }
+    }
+    run_parallel(
+        todo.size(),
+        [&](size_t w) {
+            if (g_runner.stop) return;
+            const std::string &src = job->srcs[todo[w]];
+            const auto t0 = std::chrono::steady_clock::now();
+            std::string cubin = compile_cubin(src);
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            std::lock_guard<std::mutex> lk(g_mu);
+            g_stats.compile_s += dt;
+            if (cubin.empty()) return;
+            g_stats.compiled++;
+            g_cubins.emplace(src, std::move(cubin));
+        },
+        false);
+    {
+        std::lock_guard<std::mutex> lk(job->mu);
+        job->done = true;
+    }
+    job->cv.notify_all();
+}
+}  // namespace
+
+std::shared_ptr<JitJob> jit_prefetch(std::vector<std::string> srcs) {
+    auto job = std::make_shared<JitJob>();
+    job->srcs = std::move(srcs);
+    if (!jit_available()) {
+        note_error(nvrtc().why);
+        job->done = true;
+        return job;
+    }
+    std::lock_guard<std::mutex> lk(g_runner.mu);
+    // join the workers of finished jobs
+    for (size_t i = 0; i < g_runner.threads.size();) {
+        if (g_runner.threads[i].second->done && g_runner.threads[i].first.joinable()) {
+            g_runner.threads[i].first.join();
+            g_runner.threads.erase(g_runner.threads.begin() + (std::ptrdiff_t)i);
+        } else {
+            i++;
+        }
+    }
+    g_runner.threads.emplace_back(std::thread(run_job, job), job);
+    return job;
+}
+
+bool jit_job_done(const JitJob &job) { return job.done.load(); }
+
+void jit_job_wait(JitJob &job) {
+    std::unique_lock<std::mutex> lk(job.mu);
+    job.cv.wait(lk, [&] { return job.done.load(); });
 }
 
 bool jit_sweep_kernels(const JitGeometry &geo, const std::vector<PlannedSweep> &plan, std::vector<const void *> &out) {

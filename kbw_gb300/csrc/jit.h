@@ -4,6 +4,7 @@
 
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,15 @@ const void *jit_kernel(const std::string &src, const char *entry);
 // Compile sources (entry kbwg_jit_sweep) to cubins without loading them (no
 // GPU needed), in parallel; returns how many failed.
 size_t jit_compile_only(const std::vector<std::string> &srcs);
+
+// Background compilation of sources (to cubins, not loaded): started by
+// jit_prefetch on a worker thread; jit_kernel and jit_sweep_kernels then load
+// its results without compiling.  NVRTC only; no CUDA call off the caller's
+// thread.
+struct JitJob;
+std::shared_ptr<JitJob> jit_prefetch(std::vector<std::string> srcs);
+bool jit_job_done(const JitJob &job);
+void jit_job_wait(JitJob &job);
 
 bool jit_available();
 std::string jit_last_error();

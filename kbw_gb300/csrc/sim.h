@@ -107,6 +107,10 @@ cudaError_t flush_queue(Sim &s);
 // Fusion planner entry used by flush_queue (sweep.cu).
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
 
+// Wait for the handle's background compilations of specialised kernels;
+// true if any was still to be used (a later flush of its structure loads it).
+bool wait_specialised(Sim &s);
+
 // Write and compile (NVRTC, without loading: no GPU needed) the specialised
 // kernel of every sweep a flush of `gates` would run on `s`; returns the
 // number of failed compilations and sets `sweeps`.

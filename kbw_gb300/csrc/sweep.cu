@@ -24,6 +24,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <type_traits>
 
 #include <math.h>
@@ -191,11 +192,20 @@ struct SweepGraph {
     size_t sweeps = 0;
     uint64_t last_use = 0;
 };
+// A background compilation of the specialised kernels of one structure
+// (auto mode), started on its second flush.
+struct SpecialisedJob {
+    uint64_t key = 0;                 // structure hash (with kernel and depth)
+    std::shared_ptr<JitJob> job;
+    bool used = false;                // its kernels were loaded into a flush once
+};
 struct GraphCache {
     std::vector<SweepGraph> entries;
     std::vector<uint64_t> seen;  // structure hashes flushed once (a graph is built on the second time)
+    std::vector<SpecialisedJob> jobs;
     uint64_t clock = 0;
 };
+constexpr size_t kJobEntries = 32;
 constexpr size_t kGraphCacheEntries = 8;
 
 static void free_entry(SweepGraph &g) {
@@ -261,23 +271,41 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
     // timed profiling marks every launch with events, which a graph replay cannot
     const bool graphs_ok = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
+    // auto mode: specialised kernels come from a background compilation
+    // started on a structure's second flush; until it is done the
+    // interpreted kernel runs (same amplitudes), then the structure's graph is
+    // rebuilt once with the specialised kernels
+    const bool auto_jit = s.jit_mode == KBWG_JIT_AUTO && s.n >= jit_min_qubits();
     bool repeat = false;  // this gate structure was flushed before on the handle
+    SpecialisedJob *job = nullptr;
     std::vector<uint64_t> sig;
+    uint64_t h = 0;
     if (graphs_ok || s.jit_mode == KBWG_JIT_AUTO) {
         if (!s.graphs) s.graphs = new GraphCache();
         GraphCache &gc = *(GraphCache *)s.graphs;
         sig = structure_of(gates, count);
         sig.push_back((uint64_t)(uintptr_t)kid);
         sig.push_back(depth);
-        const uint64_t h = hash_of(sig);
+        h = hash_of(sig);
         for (uint64_t x : gc.seen) repeat = repeat || x == h;
         if (!repeat) {  // first sight of this structure: launch directly, remember it
             if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
             gc.seen.push_back(h);
         }
+        if (auto_jit)
+            for (SpecialisedJob &j : gc.jobs)
+                if (j.key == h) job = &j;
+        const bool jit_ready = job && !job->used && jit_job_done(*job->job);
         if (graphs_ok)
-            for (SweepGraph &g : gc.entries) {
+            for (size_t gi = 0; gi < gc.entries.size(); gi++) {
+                SweepGraph &g = gc.entries[gi];
                 if (g.kernel != kid || g.sig != sig) continue;
+                if (jit_ready && g.specialised == 0) {  // rebuild it with the specialised kernels
+                    cudaStreamSynchronize(s.stream);    // its program buffer may still be read
+                    free_entry(g);
+                    gc.entries.erase(gc.entries.begin() + (long)gi);
+                    break;
+                }
                 cudaError_t e = upload_program<P>(s, g.planned, g.src, gates, g.dprog);
                 if (e != cudaSuccess) return e;
                 e = cudaGraphLaunch(g.exec, s.stream);
@@ -323,8 +351,24 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     // graph), or on every flush in KBWG_JIT_ALWAYS mode.  A sweep whose kernel
     // could not be built runs the interpreted k_sweep.
     std::vector<const void *> jk;
-    if (s.jit_mode == KBWG_JIT_ALWAYS || (s.jit_mode == KBWG_JIT_AUTO && repeat && s.n >= jit_min_qubits())) {
-        const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+    bool load_jit = s.jit_mode == KBWG_JIT_ALWAYS;
+    if (auto_jit && repeat) {
+        if (!job) {  // start compiling this structure's kernels in the background
+            std::vector<std::string> srcs;
+            for (const PlannedSweep &sw : plan) srcs.push_back(jit_sweep_source(geo, sw));
+            GraphCache &gc = *(GraphCache *)s.graphs;
+            if (gc.jobs.size() >= kJobEntries) gc.jobs.erase(gc.jobs.begin());
+            SpecialisedJob nj;
+            nj.key = h;
+            nj.job = jit_prefetch(std::move(srcs));
+            gc.jobs.push_back(nj);
+        } else if (jit_job_done(*job->job)) {
+            load_jit = true;
+            job->used = true;
+        }
+    }
+    if (load_jit) {
         jit_sweep_kernels(geo, plan, jk);
         for (const void *f : jk) {
             if (!f) continue;
@@ -570,6 +614,18 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
     }
     if (gr != 1.0 || gi != 0.0) emit_scale();
     return out;
+}
+
+bool wait_specialised(Sim &s) {
+    GraphCache *gc = (GraphCache *)s.graphs;
+    if (!gc) return false;
+    bool waited = false;
+    for (SpecialisedJob &j : gc->jobs)
+        if (!j.used) {
+            jit_job_wait(*j.job);
+            waited = true;
+        }
+    return waited;
 }
 
 bool ff_capable(const Sim &s) {

@@ -51,7 +51,8 @@ Key key_of(const Sim &s, const std::vector<GateDesc> &g) {
 
 // Device time of `reps` applications of the circuit with the handle's
 // current settings, after two untimed ones (the first plans and launches
-// directly, the second records the CUDA graph that later ones replay).
+// directly, the second records the CUDA graph that later ones replay and
+// starts compiling the specialised kernels, and a third takes them in).
 int32_t time_runs(Sim &s, const std::vector<GateDesc> &g, uint32_t reps, cudaEvent_t e0, cudaEvent_t e1, double &ms,
                   std::string &err) {
     auto cuda_fail = [&](cudaError_t e, const char *what) {
@@ -61,6 +62,10 @@ int32_t time_runs(Sim &s, const std::vector<GateDesc> &g, uint32_t reps, cudaEve
     cudaError_t e;
     for (int w = 0; w < 2; w++)
         if ((e = run_fused(s, g.data(), g.size())) != cudaSuccess) return cuda_fail(e, "tuning run");
+    // the second run started compiling the specialised kernels of these
+    // settings (auto mode): wait, and run once more to take them into the graph
+    if (wait_specialised(s) && (e = run_fused(s, g.data(), g.size())) != cudaSuccess)
+        return cuda_fail(e, "tuning run");
     if ((e = cudaEventRecord(e0, s.stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     for (uint32_t r = 0; r < reps; r++)
         if ((e = run_fused(s, g.data(), g.size())) != cudaSuccess) return cuda_fail(e, "tuning run");

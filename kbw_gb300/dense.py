@@ -267,6 +267,11 @@ class DenseGB300:
         """Run-time specialised sweep kernels: N.JIT_OFF, N.JIT_AUTO or N.JIT_ALWAYS."""
         N.check(self._lib.kbwg_set_jit(self._h, int(mode)))
 
+    def jit_wait(self):
+        """Wait for the handle's background compilations of specialised
+        kernels (auto mode): the next flush of each structure runs them."""
+        N.check(self._lib.kbwg_jit_wait(self._h))
+
     def jit_info(self):
         """The handle's JIT mode, how many sweeps of its last flush ran a
         specialised kernel, and the process-wide compile statistics."""

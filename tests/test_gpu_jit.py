@@ -99,7 +99,7 @@ def test_consecutive_hadamards_on_register_bits():
     assert np.array_equal(bits(out[1]), bits(want))
 
 
-def test_auto_mode_second_flush_and_replay():
+def test_auto_mode_background_compile_and_replay():
     n = 20  # the default threshold of the auto mode
     circ1 = C.brickwork(n, 4, 11)
     # the same structure with other rotation angles
@@ -108,19 +108,23 @@ def test_auto_mode_second_flush_and_replay():
     auto = DenseGB300(n, "c128", fast_c128=True, jit=N.JIT_AUTO)
     off = DenseGB300(n, "c128", fast_c128=True, jit=N.JIT_OFF)
     seen = []
-    for circ in (circ1, circ2, circ1, circ2):
+    for i, circ in enumerate((circ1, circ2, circ1, circ2, circ1)):
+        if i == 2:
+            auto.jit_wait()  # the second flush started the compilation
         for sim in (auto, off):
             sim.apply(circ)
             sim.flush()
         _, passes = auto.last_flush_stats()
         seen.append((auto.jit_info()["last_specialised"], passes))
         assert np.array_equal(bits(auto.state()), bits(off.state()))
-    # first sight: interpreted; the second flush builds the graph with
-    # specialised kernels; later flushes replay it
-    assert seen[0][0] == 0
-    for spec, passes in seen[1:]:
+    # first sight: interpreted; second: interpreted while its kernels compile
+    # (the graph is built); after the wait the graph is rebuilt with the
+    # specialised kernels and later flushes replay it
+    assert seen[0][0] == 0 and seen[1][0] == 0
+    for spec, passes in seen[2:]:
         assert spec == passes > 0
     assert auto.jit_info()["mode"] == N.JIT_AUTO
+    assert N.jit_info()["failed"] == 0, N.jit_last_error()
 
 
 def test_auto_mode_skips_small_registers():
