@@ -6,7 +6,7 @@
  * `QuantumExecution` (kbw src/quantum_execution.rs:48-162) or one piece of the
  * `QubitManager` adapter built on it (src/quantum_execution.rs:171-427); the
  * citation is given per entry.  A Rust `QuantumExecution` impl binds these
- * symbols one to one (see INTEGRATION.md), exactly as the reference's
+ * symbols one to one, exactly as the reference's
  * `kbw_make_configuration` (kbw.h:48-54, src/c_api.rs:60-129) binds its own
  * backends.
  *
@@ -444,7 +444,9 @@ int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, 
  * scratch is a fixed 8 KiB device array in this library (608 partial sums
  * and a ticket), held by every GPU that loads the library until exit.
  * Limits: num_qubits <= 32 (KBWG_EQUBITS otherwise); value must lie inside
- * mask (KBWG_EINVAL).  The first call on a device looks up the array's device
+ * mask, and state and out must be device (or managed) memory of the current
+ * device (KBWG_EINVAL otherwise).  The first call in a CUDA context (per
+ * device, and again after a cudaDeviceReset) looks up the array's device
  * address with that device current (kbwg_select_device), so make it before
  * any stream capture.  All calls share the array: calls that overlap on the
  * GPU (other streams, other threads) race; serialise them. */

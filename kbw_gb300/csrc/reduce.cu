@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "../../include/kbwg.h"
 #include "ff.cuh"
@@ -944,24 +945,67 @@ static_assert(kNoAllocTicketOffset + 256 <= kNoAllocScratchBytes, "ticket overfl
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Host code may not use g_noalloc_scratch as an address (it names a host-side
-// stand-in); the device address is looked up once per device.
-static std::mutex g_noalloc_mu;
-static void *g_noalloc_addr[256];
+// stand-in); the device address is looked up with the device current, once
+// per CUDA context.  The cache is keyed on the context's id, not on the
+// device ordinal: after cudaDeviceReset the device gets a new context in
+// which the array may have another address.
+namespace {
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+std::mutex g_noalloc_mu;
+std::vector<std::pair<unsigned long long, void *>> g_noalloc_addr;  // context id -> array address
+
+// Id of the calling thread's current CUDA context (driver entry points
+// obtained through the runtime); false if none is current or unknown.
+bool current_context_id(unsigned long long &id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        resolved = true;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&get_current, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess || q != cudaDriverEntryPointSuccess)
+            get_current = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&get_id, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess || q != cudaDriverEntryPointSuccess)
+            get_id = nullptr;
+    }
+    void *ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, &id) == 0;
+}
+}  // namespace
 
 static cudaError_t noalloc_scratch(void **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_addr[dev] = p;
-    }
-    *out = g_noalloc_addr[dev];
+    unsigned long long id = 0;
+    if (current_context_id(id))
+        for (const auto &a : g_noalloc_addr)
+            if (a.first == id) {
+                *out = a.second;
+                return cudaSuccess;
+            }
+    // set-up on this context (the lookup makes the current device's context current if none is)
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    if (current_context_id(id)) g_noalloc_addr.emplace_back(id, p);
+    *out = p;
     return cudaSuccess;
+}
+
+// A device or managed allocation on the current device (a host pointer, or
+// memory of another device, would make the kernel fault).
+static bool on_current_device(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return false;
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && a.device == dev;
 }
 
 }  // namespace kbwg
@@ -982,9 +1026,14 @@ extern "C" int32_t kbwg_masked_norm_noalloc(const void *state, uintptr_t num_qub
         set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: bad precision");
         return KBWG_EINVAL;
     }
-    const uint64_t all = (num_qubits >= 64) ? ~0ull : ((1ull << num_qubits) - 1);
+    const uint64_t all = (1ull << num_qubits) - 1;  // num_qubits <= 32 here
     if ((mask & ~all) || (value & ~mask)) {
         set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: mask/value outside the register or value outside mask");
+        return KBWG_EINVAL;
+    }
+    if (!on_current_device(state) || !on_current_device(out)) {
+        set_error(KBWG_EINVAL, "kbwg_masked_norm_noalloc: state and out must be device (or managed) memory of the "
+                               "current device");
         return KBWG_EINVAL;
     }
     void *base = nullptr;

@@ -188,3 +188,25 @@ def test_specialised_sweep_kernels_compile(lib, prec, flags, tile):
         raise
     assert sweeps > 0
     assert failed == 0, N.jit_last_error()
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_planner_long_lists_and_stage_limit(lib, prec):
+    """Past the planner's 8192-gate selection window, and with sweeps that
+    hit the 48-stage limit (gates that alternate between the two register
+    layouts and do not commute): every gate placed exactly once, and the
+    planned order gives the program-order state on the oracle."""
+    n = 14
+    circ = C.random_circuit(n, 9000, 77, max_controls=2)
+    # each gate needs the other layout and shares a qubit non-diagonally with the last
+    circ += [(C.X, 12, (5,), 0.0), (C.X, 5, (12,), 0.0)] * 60
+    circ += C.random_circuit(n, 300, 78, max_controls=1)
+    sweeps = plan(n, circ, prec)
+    order = [i for _, idx in sweeps for i in idx]
+    assert sorted(order) == list(range(len(circ)))
+    o = oracle.OracleDense(n, prec)
+    o.apply([circ[i] for i in order])
+    ref = oracle.OracleDense(n, prec)
+    ref.apply(circ)
+    tol = 1e-12 if prec == "c128" else 1e-4
+    assert rel_err(o.state(), ref.state()) < tol

@@ -29,12 +29,14 @@ def _noalloc(lib, ptr, n, prec_code, mask, value, out_ptr, stream):
                                         ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream))
 
 
-@pytest.mark.parametrize("prec", ["c128", "c64"])
-def test_noalloc_matches_measure_p1_twice(prec):
+@pytest.mark.parametrize("prec,fast", [("c128", False), ("c64", False), ("c128", True)])
+def test_noalloc_matches_measure_p1_twice(prec, fast):
+    # fast: a complex128 handle that keeps its state in float-float form
+    # between sweeps; reading its device pointer turns it back to binary64
     torch = pytest.importorskip("torch")
     lib = N.load()
     n = 18
-    sim = DenseGB300(n, prec)
+    sim = DenseGB300(n, prec, fast_c128=fast)
     sim.apply(C.random_circuit(n, 300, 23, max_controls=2))
     nq, prec_code, ptr, _ = sim.device_info()  # flushes the gate queue
     stream = sim.stream_handle()
@@ -71,3 +73,9 @@ def test_noalloc_rejects_out_of_range():
     assert _noalloc(lib, ptr, 4, prec_code, 1, 2, out.data_ptr(), 0) == N.EINVAL
     assert _noalloc(lib, ptr, 4, prec_code, 1 << 5, 0, out.data_ptr(), 0) == N.EINVAL
     assert _noalloc(lib, 0, 4, prec_code, 1, 1, out.data_ptr(), 0) == N.EINVAL
+    # host memory for the state or the output is refused, not handed to the kernel
+    host = np.zeros(64, dtype=np.complex64)
+    hout = np.zeros(1, dtype=np.float64)
+    assert _noalloc(lib, host.ctypes.data, 4, prec_code, 1, 1, out.data_ptr(), 0) == N.EINVAL
+    assert _noalloc(lib, ptr, 4, prec_code, 1, 1, hout.ctypes.data, 0) == N.EINVAL
+    assert _noalloc(lib, ptr, 4, prec_code, 1, 1, out.data_ptr(), 0) == N.OK
