@@ -430,6 +430,11 @@ int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, 
                        uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uintptr_t *n_sweeps,
                        uintptr_t *n_failed);
 
+/* The same for the specialised reverse sweeps of kbwg_adjoint_gradient on
+ * `gates` (one segment, every P/RX/RY/RZ gate differentiated). */
+int32_t kbwg_jit_check_adjoint(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                               uintptr_t n_gates, uintptr_t *n_sweeps, uintptr_t *n_failed);
+
 /* ---- allocation-free entry (no counterpart in the reference) ------------- */
 
 /* For callers that cannot allocate device memory: code recorded into a CUDA

@@ -115,6 +115,7 @@ SIGNATURES = {
     "kbwg_jit_last_error": (ctypes.c_char_p, []),
     "kbwg_jit_check": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,
                               _UP, _UP]),
+    "kbwg_jit_check_adjoint": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, _UP, _UP]),
     "kbwg_masked_norm_noalloc": (_I32, [_P, _U, _I32, ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "kbwg_last_error": (ctypes.c_char_p, []),
     "kbwg_launch_count": (ctypes.c_uint64, []),
@@ -182,6 +183,16 @@ def jit_check(num_qubits, prec, flags, gates, tile_qubits=0, fusion_depth=0):
     nf = ctypes.c_size_t()
     check(load().kbwg_jit_check(int(num_qubits), prec, int(flags), int(tile_qubits), int(fusion_depth), gates,
                                 len(gates), ctypes.byref(ns), ctypes.byref(nf)))
+    return int(ns.value), int(nf.value)
+
+
+def jit_check_adjoint(num_qubits, prec, flags, gates):
+    """Compile (NVRTC, no GPU) the specialised reverse sweeps of an adjoint
+    gradient of `gates`; returns (sweeps, failed)."""
+    ns = ctypes.c_size_t()
+    nf = ctypes.c_size_t()
+    check(load().kbwg_jit_check_adjoint(int(num_qubits), prec, int(flags), gates, len(gates), ctypes.byref(ns),
+                                        ctypes.byref(nf)))
     return int(ns.value), int(nf.value)
 
 

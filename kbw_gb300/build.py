@@ -40,7 +40,7 @@ def headers():
 
 # Device headers compiled again at run time by NVRTC (csrc/jit.cpp): embedded
 # in the library as string literals so that it needs no source tree.
-JIT_HEADERS = ["common.cuh", "sweep.h", "ff.cuh", "ff2.cuh", "sweep_dev.cuh", "jit_dev.cuh"]
+JIT_HEADERS = ["common.cuh", "sweep.h", "ff.cuh", "ff2.cuh", "sweep_dev.cuh", "jit_dev.cuh", "adjoint_dev.cuh"]
 JIT_INC = os.path.join(OBJ, "jit_sources.inc")
 
 

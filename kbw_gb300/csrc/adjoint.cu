@@ -23,15 +23,24 @@
 #include <string.h>
 
 #include <algorithm>
+#include <string>
 #include <type_traits>
 #include <vector>
 
 #include "../../include/kbwg.h"
 #include "kernels.h"
 #include "sim.h"
+#include "adjoint_dev.cuh"
+#include "jit.h"
 #include "sweep_dev.cuh"
 
 namespace kbwg {
+
+// C++ names of the adjoint's arithmetic policies, for its specialised kernels.
+template <class P> struct AdjPolicyName;
+template <> struct AdjPolicyName<FastP> { static constexpr const char *s = "kbwg::FastP"; };
+template <> struct AdjPolicyName<FF2B> { static constexpr const char *s = "kbwg::FF2B"; };
+template <> struct AdjPolicyName<Fast<double>> { static constexpr const char *s = "kbwg::Fast<double>"; };
 
 // ---- lambda = H phi ------------------------------------------------------------------
 // One group of strings with common flip mask x:
@@ -192,225 +201,6 @@ __global__ void __launch_bounds__(256) k_inner_re(const cx<T> *__restrict__ a, c
         }
     }
 }
-
-// ---- gradient terms --------------------------------------------------------------------
-// Contribution of one amplitude (lam, phi) whose pair partner is phip, on
-// the |one> side of the target bit:
-//   X: Im(conj(lam) phip)          Y: (one ? +1 : -1) Re(conj(lam) phip)
-//   Z: (one ? -1 : +1) Im(conj(lam) phi)     P1: one ? -2 Im(conj(lam) phi) : 0
-template <class P> struct Grad;
-
-template <class T>
-struct Grad<Fast<T>> {
-    using Amp = cx<T>;
-    using Acc = T;
-    static __device__ __forceinline__ Acc zero() { return (T)0; }
-    static __device__ __forceinline__ Acc term(int gt, bool one, Amp l, Amp p, Amp pp) {
-        switch (gt) {
-        case GT_X: return l.re * pp.im - l.im * pp.re;
-        case GT_Y: {
-            const T r = l.re * pp.re + l.im * pp.im;
-            return one ? r : -r;
-        }
-        case GT_Z: {
-            const T r = l.re * p.im - l.im * p.re;
-            return one ? -r : r;
-        }
-        default: return one ? (T)-2 * (l.re * p.im - l.im * p.re) : (T)0;
-        }
-    }
-    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
-    static __device__ __forceinline__ Acc warp_sum(Acc a) {
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        return a;
-    }
-    // per-warp accumulator across tiles: float-float for complex64 (no FP64
-    // instruction in the sweep), binary64 for complex128
-    using Wacc = typename std::conditional<sizeof(T) == 4, ff::f2, double>::type;
-    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) {
-        if constexpr (sizeof(T) == 4) return ff::add(w, ff::f2{a, 0.f});
-        else return w + a;
-    }
-    static __device__ __forceinline__ double wvalue(Wacc w) {
-        if constexpr (sizeof(T) == 4) return (double)w.h + (double)w.l;
-        else return w;
-    }
-};
-
-template <>
-struct Grad<FFPol> {
-    using Amp = FFPol::Amp;
-    using Acc = ff::f2;
-    static __device__ __forceinline__ Acc zero() { return ff::f2{0.f, 0.f}; }
-    static __device__ __forceinline__ ff::f2 im_conj(const Amp &l, const Amp &b) {  // Im(conj(l) b)
-        return ff::dot2(l.re, b.im, ff::neg(l.im), b.re);
-    }
-    static __device__ __forceinline__ ff::f2 re_conj(const Amp &l, const Amp &b) {  // Re(conj(l) b)
-        return ff::dot2(l.re, b.re, l.im, b.im);
-    }
-    static __device__ __forceinline__ Acc term(int gt, bool one, const Amp &l, const Amp &p, const Amp &pp) {
-        switch (gt) {
-        case GT_X: return im_conj(l, pp);
-        case GT_Y: {
-            const ff::f2 r = re_conj(l, pp);
-            return one ? r : ff::neg(r);
-        }
-        case GT_Z: {
-            const ff::f2 r = im_conj(l, p);
-            return one ? ff::neg(r) : r;
-        }
-        default: {
-            if (!one) return zero();
-            const ff::f2 r = im_conj(l, p);
-            return ff::f2{-2.f * r.h, -2.f * r.l};
-        }
-        }
-    }
-    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return ff::add(a, b); }
-    static __device__ __forceinline__ Acc warp_sum(Acc a) {
-        for (int o = 16; o > 0; o >>= 1) {
-            Acc b{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
-            a = ff::add(a, b);
-        }
-        return a;
-    }
-    using Wacc = ff::f2;
-    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return ff::add(w, a); }
-    static __device__ __forceinline__ double wvalue(Wacc w) { return (double)w.h + (double)w.l; }
-};
-
-// Packed complex64 amplitudes (float2 re, im): the terms of Fast<float>.
-template <>
-struct Grad<FastP> {
-    using Amp = FastP::Amp;
-    using G1 = Grad<Fast<float>>;
-    using Acc = G1::Acc;
-    static __device__ __forceinline__ cx<float> unpack(Amp a) { return cx<float>{a.x, a.y}; }
-    static __device__ __forceinline__ Acc zero() { return G1::zero(); }
-    static __device__ __forceinline__ Acc term(int gt, bool one, Amp l, Amp p, Amp pp) {
-        return G1::term(gt, one, unpack(l), unpack(p), unpack(pp));
-    }
-    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return G1::add(a, b); }
-    static __device__ __forceinline__ Acc warp_sum(Acc a) { return G1::warp_sum(a); }
-    using Wacc = G1::Wacc;
-    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return G1::wadd(w, a); }
-    static __device__ __forceinline__ double wvalue(Wacc w) { return G1::wvalue(w); }
-};
-
-// Packed float-float amplitudes: the terms of FFPol on the unpacked pairs.
-template <>
-struct Grad<FF2B> {
-    using Amp = FF2B::Amp;
-    using G1 = Grad<FFPol>;
-    using Acc = G1::Acc;
-    static __device__ __forceinline__ FFPol::Amp unpack(const Amp &a) {
-        return FFPol::Amp{ff::f2{a.h.x, a.l.x}, ff::f2{a.h.y, a.l.y}};
-    }
-    static __device__ __forceinline__ Acc zero() { return G1::zero(); }
-    static __device__ __forceinline__ Acc term(int gt, bool one, const Amp &l, const Amp &p, const Amp &pp) {
-        return G1::term(gt, one, unpack(l), unpack(p), unpack(pp));
-    }
-    static __device__ __forceinline__ Acc add(Acc a, Acc b) { return G1::add(a, b); }
-    static __device__ __forceinline__ Acc warp_sum(Acc a) { return G1::warp_sum(a); }
-    using Wacc = G1::Wacc;
-    static __device__ __forceinline__ Wacc wadd(Wacc w, Acc a) { return G1::wadd(w, a); }
-    static __device__ __forceinline__ double wvalue(Wacc w) { return G1::wvalue(w); }
-};
-
-template <class P, int R, int B>
-__device__ __forceinline__ typename Grad<P>::Acc grad_pairs(int gt, const typename P::Amp (&ph)[1 << R],
-                                                           const typename P::Amp (&la)[1 << R], uint32_t creg) {
-    using G = Grad<P>;
-    typename G::Acc acc = G::zero();
-#pragma unroll
-    for (int jj = 0; jj < (1 << (R - 1)); jj++) {
-        const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
-        const int j1 = j0 | (1 << B);
-        if (creg == 0u || ((uint32_t)j0 & creg) == creg) {
-            acc = G::add(acc, G::term(gt, false, la[j0], ph[j0], ph[j1]));
-            acc = G::add(acc, G::term(gt, true, la[j1], ph[j1], ph[j0]));
-        }
-    }
-    return acc;
-}
-
-// This thread's part of the gradient inner product of one step.  Every lane
-// must call it (lane-bit targets shuffle).
-template <class P, int K, int R>
-__device__ __forceinline__ typename Grad<P>::Acc grad_partial(const TileGate &g, int gt,
-                                                             const typename P::Amp (&ph)[1 << R],
-                                                             const typename P::Amp (&la)[1 << R], int R0,
-                                                             uint32_t F, uint64_t base) {
-    using G = Grad<P>;
-    constexpr int NR = 1 << R;
-    typename G::Acc acc = G::zero();
-    const uint32_t regmask = (uint32_t)(NR - 1) << R0;
-    const uint32_t fixed_need = g.cl & ~regmask;
-    const bool fok = (F & fixed_need) == fixed_need;
-    const uint32_t creg = (g.cl & regmask) >> R0;
-    const uint32_t tb = g.tb;
-    if (gt == GT_Z || gt == GT_P1) {
-        if (!fok) return acc;
-        const int rb = (int)tb - R0;
-        if (tb != TG_OUTER && rb >= 0 && rb < R) {
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (creg == 0u || ((uint32_t)j & creg) == creg)
-                    acc = G::add(acc, G::term(gt, ((j >> rb) & 1) != 0, la[j], ph[j], ph[j]));
-        } else {
-            const bool one = (tb == TG_OUTER) ? (((base >> g.tout) & 1ull) != 0) : (((F >> tb) & 1u) != 0);
-#pragma unroll
-            for (int j = 0; j < NR; j++)
-                if (creg == 0u || ((uint32_t)j & creg) == creg) acc = G::add(acc, G::term(gt, one, la[j], ph[j], ph[j]));
-        }
-        return acc;
-    }
-    if (tb < (uint32_t)kLaneBits) {
-        const bool one = ((F >> tb) & 1u) != 0;
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            const typename P::Amp pp = P::shfl(ph[j], 1 << tb);
-            if (fok && (creg == 0u || ((uint32_t)j & creg) == creg)) acc = G::add(acc, G::term(gt, one, la[j], ph[j], pp));
-        }
-        return acc;
-    }
-    if (!fok) return acc;
-    switch ((int)tb - R0) {
-    case 0: return grad_pairs<P, R, 0>(gt, ph, la, creg);
-    case 1: return grad_pairs<P, R, 1>(gt, ph, la, creg);
-    case 2: return grad_pairs<P, R, 2>(gt, ph, la, creg);
-    default:
-        if constexpr (R > 3) return grad_pairs<P, R, (R > 3 ? 3 : 0)>(gt, ph, la, creg);
-        return acc;
-    }
-}
-
-// ---- two-state adjoint sweep -------------------------------------------------------------
-template <class T> struct AdjCfg;
-template <> struct AdjCfg<float> {
-    static constexpr int K = 12, R = 4;
-};
-template <> struct AdjCfg<double> {
-    static constexpr int K = 11, R = 3;
-};
-
-struct AdjParams {
-    SweepParams sw;
-    const uint32_t *ginfo;  // per program gate: gradient type | (slot << 4)
-    double *partials;       // [gridDim.x][nslots]
-    uint32_t nslots;
-};
-
-template <class P, int K, int R>
-struct AdjKernel {
-    using Mem = typename P::Mem;
-    static constexpr int kThreads = 32 << (K - kLaneBits - R);
-    static constexpr int kWarps = kThreads / 32;
-    static constexpr size_t kTileBytes = sizeof(Mem) << K;
-    static constexpr size_t kSmem = 2 * kTileBytes + 256 * sizeof(uint64_t) + kMaxSweepGates * sizeof(TileGate) +
-                                    kMaxSweepGates * sizeof(uint32_t) + (size_t)kWarps * kMaxSweepGates * sizeof(double) +
-                                    16;
-};
 
 template <class P, int K, int R>
 __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
@@ -621,14 +411,15 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<P, K, R>, AK::kThreads, AK::kSmem);
     if (e != cudaSuccess) return e;
     const uint64_t tiles = 1ull << (s.n - K);
-    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * std::max(occ, 1));
-    for (const PlannedSweep &sw : plan) {
-        const size_t ng = sw.gates.size();
-        std::vector<TileGate> prog = sw.gates;
-        for (TileGate &t : prog) P::pack_host(t);
-        std::vector<uint32_t> meta(2 * kMaxSweepGates, 0);  // ginfo | gate_of_slot
+    // gradient info per sweep: type | slot << 4 per gate, and the gate of each slot
+    std::vector<std::vector<uint32_t>> metas(plan.size());
+    std::vector<uint32_t> slots(plan.size(), 0);
+    for (size_t k = 0; k < plan.size(); k++) {
+        const PlannedSweep &sw = plan[k];
+        std::vector<uint32_t> &meta = metas[k];
+        meta.assign(2 * kMaxSweepGates, 0);
         uint32_t nslots = 0;
-        for (size_t i = 0; i < ng; i++) {
+        for (size_t i = 0; i < sw.gates.size(); i++) {
             const size_t j = rev_src[sw.src[i]];
             if (gtype[j] != GT_NONE) {
                 meta[i] = (uint32_t)gtype[j] | (nslots << 4);
@@ -636,6 +427,34 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
                 nslots++;
             }
         }
+        slots[k] = nslots;
+    }
+    // run-time specialised reverse sweeps (the handle's JIT mode, as for the
+    // forward sweeps); a sweep without one runs the compiled k_adjoint
+    std::vector<const void *> jk;
+    if (s.jit_mode != KBWG_JIT_OFF) {
+        const JitGeometry geo{AdjPolicyName<P>::s, K, R, AK::kThreads, 2};
+        std::vector<std::string> srcs;
+        for (size_t k = 0; k < plan.size(); k++) srcs.push_back(jit_adjoint_source(geo, plan[k], metas[k]));
+        jk = specialised_kernels(s, srcs, "kbwg_jit_adjoint");
+        for (const void *f : jk) {
+            if (!f) continue;
+            e = ensure_smem_limit(f, AK::kSmem);
+            if (e != cudaSuccess) return e;
+            int o = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, f, AK::kThreads, AK::kSmem);
+            if (e != cudaSuccess) return e;
+            occ = std::min(occ, std::max(o, 1));  // one grid size for both kernels (partials buffer)
+        }
+    }
+    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * std::max(occ, 1));
+    for (size_t k = 0; k < plan.size(); k++) {
+        const PlannedSweep &sw = plan[k];
+        const size_t ng = sw.gates.size();
+        std::vector<TileGate> prog = sw.gates;
+        for (TileGate &t : prog) P::pack_host(t);
+        const std::vector<uint32_t> &meta = metas[k];
+        const uint32_t nslots = slots[k];
         e = copy_async(bufs.prog, prog.data(), ng * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
         if (e != cudaSuccess) return e;
         e = copy_async(bufs.meta, meta.data(), meta.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s.stream);
@@ -659,7 +478,15 @@ static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<G
         a.partials = bufs.partials;
         a.nslots = nslots;
         if (s.prof.on) s.prof.mark(s.stream);
-        k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)bufs.lam, a);
+        const void *spec = jk.empty() ? nullptr : jk[k];
+        if (spec) {
+            Mem *ph = (Mem *)s.state, *la = (Mem *)bufs.lam;
+            void *args[] = {(void *)&ph, (void *)&la, (void *)&a};
+            cudaLaunchKernel(spec, dim3((unsigned)grid), dim3(AK::kThreads), args, AK::kSmem, s.stream);
+        } else {
+            k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)bufs.lam,
+                                                                                    a);
+        }
         count_launch();
         e = cudaGetLastError();
         if (s.prof.on) {
@@ -878,6 +705,46 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
     if (e != cudaSuccess) return fail_cuda(e, "finish");
     bufs.release();
     return KBWG_OK;
+}
+
+// ---- compile-only check of the specialised reverse sweeps (no GPU) ----------------
+template <class P, int K, int R>
+static size_t check_adjoint_p(const Sim &s, const std::vector<GateDesc> &fwd, const std::vector<int> &gtype,
+                              size_t &sweeps) {
+    using AK = AdjKernel<P, K, R>;
+    std::vector<GateDesc> rev;
+    std::vector<size_t> rev_src;
+    for (size_t j = fwd.size(); j-- > 0;) {
+        rev.push_back(fwd[j]);  // (the structure of the inverse gate is the gate's)
+        rev_src.push_back(j);
+    }
+    const std::vector<PlannedSweep> plan = plan_sweeps(s.n, K, R, rev.data(), rev.size(), false);
+    const JitGeometry geo{AdjPolicyName<P>::s, K, R, AK::kThreads, 2};
+    std::vector<std::string> srcs;
+    for (const PlannedSweep &sw : plan) {
+        std::vector<uint32_t> meta(sw.gates.size(), 0);
+        uint32_t nslots = 0;
+        for (size_t i = 0; i < sw.gates.size(); i++) {
+            const size_t j = rev_src[sw.src[i]];
+            if (gtype[j] != GT_NONE) meta[i] = (uint32_t)gtype[j] | (nslots++ << 4);
+        }
+        srcs.push_back(jit_adjoint_source(geo, sw, meta));
+    }
+    sweeps = plan.size();
+    return jit_compile_only(srcs);
+}
+
+size_t jit_check_adjoint(const Sim &s, const std::vector<GateDesc> &fwd, const std::vector<int> &gtype,
+                         size_t &sweeps) {
+    sweeps = 0;
+    if (s.prec == 0) {
+        if (s.n < (uint32_t)AdjCfg<float>::K) return 0;
+        return check_adjoint_p<FastP, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, gtype, sweeps);
+    }
+    if (s.n < (uint32_t)AdjCfg<double>::K) return 0;
+    if (s.flags & KBWG_FLAG_FAST_C128)
+        return check_adjoint_p<FF2B, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, gtype, sweeps);
+    return check_adjoint_p<Fast<double>, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, gtype, sweeps);
 }
 
 int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,

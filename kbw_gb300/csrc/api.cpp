@@ -1011,6 +1011,40 @@ int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, 
     GUARD_END
 }
 
+int32_t kbwg_jit_check_adjoint(uintptr_t num_qubits, int32_t precision, uint32_t flags, const kbwg_gate *gates,
+                               uintptr_t n_gates, uintptr_t *n_sweeps, uintptr_t *n_failed) {
+    GUARD_BEGIN
+    if (!n_sweeps || !n_failed || (n_gates && !gates)) return fail(KBWG_EINVAL, "null argument");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    if (!jit_available()) return fail(KBWG_EUNSUPPORTED, "NVRTC (libnvrtc.so.13) not found");
+    Sim tmp;
+    tmp.n = (uint32_t)num_qubits;
+    tmp.prec = precision;
+    tmp.flags = flags;
+    std::vector<GateDesc> gd(n_gates);
+    std::vector<int> gtype(n_gates, GT_NONE);
+    for (uintptr_t i = 0; i < n_gates; i++) {
+        const kbwg_gate &g = gates[i];
+        if (g.kind > KBWG_RZ || g.target >= num_qubits || (g.control_mask >> num_qubits) ||
+            (g.control_mask & (1ull << g.target)))
+            return fail(KBWG_EINVAL, "bad gate");
+        gd[i] = make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle);
+        switch (g.kind) {
+        case KBWG_RX: gtype[i] = GT_X; break;
+        case KBWG_RY: gtype[i] = GT_Y; break;
+        case KBWG_RZ: gtype[i] = GT_Z; break;
+        case KBWG_P: gtype[i] = GT_P1; break;
+        default: break;
+        }
+    }
+    size_t sweeps = 0;
+    *n_failed = jit_check_adjoint(tmp, gd, gtype, sweeps);
+    *n_sweeps = sweeps;
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_select_device(int32_t device) {
     CUDA_TRY(cudaSetDevice(device));
     return KBWG_OK;

@@ -243,26 +243,95 @@ uint32_t jit_min_qubits() {
     return q;
 }
 
+namespace {
+
+// The constants expression of gate i (a load of its program entry, or the
+// zero constants for a gate that needs none).
+std::string constants_of(const TileGate &t, size_t i) {
+    const bool needs_k = !(t.cls == TG_X || t.cls == TG_Y || t.cls == TG_Z || t.cls == TG_PI ||
+                           (t.cls == TG_H && t.sub == 1));
+    if (!needs_k) return "kz";
+    char buf[64];
+    snprintf(buf, sizeof buf, "P::load(sg[%zu])", i);
+    return buf;
+}
+
+// Predicate of the controls on this stage's lane/warp bits ("true" if none).
+std::string fok_of(const TileGate &t) {
+    if (!t.fneed) return "true";
+    char buf[96];
+    snprintf(buf, sizeof buf, "((F & 0x%xu) == 0x%xu)", t.fneed, t.fneed);
+    return buf;
+}
+
+// Side of a diagonal gate's target that is fixed per thread (DFIX gates).
+std::string side_of(const TileGate &t) {
+    char buf[96];
+    if (t.cls == TG_SCALE)
+        snprintf(buf, sizeof buf, "true");
+    else if (t.tb == TG_OUTER)
+        snprintf(buf, sizeof buf, "((base >> %u) & 1u) != 0u", (unsigned)t.tout);
+    else
+        snprintf(buf, sizeof buf, "((F >> %u) & 1u) != 0u", (unsigned)t.tb);
+    return buf;
+}
+
+// Statement applying gate t (constants in `k`) to the registers `v`; the
+// control outside the tile is left to the caller.
+std::string gate_stmt(const TileGate &t, const char *v, const char *k) {
+    char buf[512];
+    const char *cls = kClassName[t.cls];
+    const int q = (t.cls == TG_PI) ? (int)t.c[0] : 0;
+    if (t.op < OP_REG) {
+        snprintf(buf, sizeof buf, "jit::lane<P, R, %d, %s, 0x%xu, %d>(%s, %s, %s, F);", (int)t.tb, cls, t.creg,
+                 (int)t.sub, v, k, fok_of(t).c_str());
+        return buf;
+    }
+    if (t.op < OP_DREG)
+        snprintf(buf, sizeof buf, "jit::reg<P, R, %d, %s, 0x%xu, %d>(%s, %s);", (int)t.rb, cls, (unsigned)t.jm,
+                 (int)t.sub, v, k);
+    else if (t.op < OP_DFIX)
+        snprintf(buf, sizeof buf, "jit::dreg<P, R, %d, %s, 0x%xu, %d>(%s, %s);", (int)t.rb, cls, (unsigned)t.jm, q, v,
+                 k);
+    else
+        snprintf(buf, sizeof buf, "jit::dfix<P, R, %s, 0x%xu, %d>(%s, %s, %s);", cls, (unsigned)t.jm, q, v, k,
+                 side_of(t).c_str());
+    std::string st = buf;
+    if (t.fneed) st = "if (" + fok_of(t) + ") { " + st + " }";
+    return st;
+}
+
+// Guard of a gate with controls outside the tile (uniform over the tile).
+std::string outer_guard(const TileGate &t, const std::string &body, bool wide) {
+    if (!t.co) return body;
+    char buf[128];
+    if (wide)
+        snprintf(buf, sizeof buf, "if ((base & 0x%llxull) == 0x%llxull) { ", (unsigned long long)t.co,
+                 (unsigned long long)t.co);
+    else
+        snprintf(buf, sizeof buf, "if ((base & 0x%xu) == 0x%xu) { ", (uint32_t)t.co, (uint32_t)t.co);
+    return std::string(buf) + body + " }";
+}
+
+}  // namespace
+
 std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
     std::string s;
     s.reserve(4096 + 160 * sw.gates.size());
     char buf[512];
     const int first = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.front();
     const int last = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.back();
-    snprintf(buf, sizeof buf,
-             "#include \"jit_dev.cuh\"\n"
-             "using namespace kbwg;\n"
-             "namespace {\n"
-             "struct Body {\n"
-             "  static constexpr int kFirst = %d, kLast = %d;\n"
-             "  template <class P, int K, int R>\n"
-             "  static __device__ __forceinline__ void run(typename P::Amp (&v)[1 << R], typename P::Amp *tile,\n"
-             "      uint32_t FA, uint32_t FB, uint32_t base, const TileGate *sg) {\n"
-             "    const typename P::K4 kz{};\n"
-             "    uint32_t F = %s;\n"
-             "    (void)tile; (void)base; (void)sg; (void)kz; (void)F;\n",
-             first, last, first == LAYOUT_A ? "FA" : "FB");
-    s += buf;
+    s += "#include \"jit_dev.cuh\"\n"
+         "using namespace kbwg;\n"
+         "namespace {\n"
+         "struct Body {\n";
+    s += "  static constexpr int kFirst = " + std::to_string(first) + ", kLast = " + std::to_string(last) + ";\n";
+    s += "  template <class P, int K, int R>\n"
+         "  static __device__ __forceinline__ void run(typename P::Amp (&v)[1 << R], typename P::Amp *tile,\n"
+         "      uint32_t FA, uint32_t FB, uint32_t base, const TileGate *sg) {\n"
+         "    const typename P::K4 kz{};\n";
+    s += std::string("    uint32_t F = ") + (first == LAYOUT_A ? "FA" : "FB") + ";\n";
+    s += "    (void)tile; (void)base; (void)sg; (void)kz; (void)F;\n";
     int layout = first;
     size_t g0 = 0;
     for (size_t st = 0; st < sw.stage_layout.size(); st++) {
@@ -276,55 +345,8 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
         const size_t g1 = sw.stage_end[st];
         for (size_t i = g0; i < g1; i++) {
             const TileGate &t = sw.gates[i];
-            const uint32_t co = (uint32_t)t.co;  // state indices fit 32 bits (at most 32 qubits)
-            const char *cls = kClassName[t.cls];
-            const bool needs_k = !(t.cls == TG_X || t.cls == TG_Y || t.cls == TG_Z || t.cls == TG_PI ||
-                                   (t.cls == TG_H && t.sub == 1));
-            char kexpr[64];
-            if (needs_k)
-                snprintf(kexpr, sizeof kexpr, "P::load(sg[%zu])", i);
-            else
-                snprintf(kexpr, sizeof kexpr, "kz");
-            const int q = (t.cls == TG_PI) ? (int)t.c[0] : 0;
-            std::string body;
-            if (t.op < OP_REG) {
-                char fok[96];
-                if (t.fneed)
-                    snprintf(fok, sizeof fok, "((F & 0x%xu) == 0x%xu)", t.fneed, t.fneed);
-                else
-                    snprintf(fok, sizeof fok, "true");
-                snprintf(buf, sizeof buf, "jit::lane<P, R, %d, %s, 0x%xu, %d>(v, %s, %s, F);", (int)t.tb, cls,
-                         t.creg, (int)t.sub, kexpr, fok);
-                body = buf;
-            } else {
-                if (t.op < OP_DREG) {
-                    snprintf(buf, sizeof buf, "jit::reg<P, R, %d, %s, 0x%xu, %d>(v, %s);", (int)t.rb, cls,
-                             (unsigned)t.jm, (int)t.sub, kexpr);
-                } else if (t.op < OP_DFIX) {
-                    snprintf(buf, sizeof buf, "jit::dreg<P, R, %d, %s, 0x%xu, %d>(v, %s);", (int)t.rb, cls,
-                             (unsigned)t.jm, q, kexpr);
-                } else {
-                    char one[96];
-                    if (t.cls == TG_SCALE)
-                        snprintf(one, sizeof one, "true");
-                    else if (t.tb == TG_OUTER)
-                        snprintf(one, sizeof one, "((base >> %u) & 1u) != 0u", (unsigned)t.tout);
-                    else
-                        snprintf(one, sizeof one, "((F >> %u) & 1u) != 0u", (unsigned)t.tb);
-                    snprintf(buf, sizeof buf, "jit::dfix<P, R, %s, 0x%xu, %d>(v, %s, %s);", cls, (unsigned)t.jm, q,
-                             kexpr, one);
-                }
-                body = buf;
-                if (t.fneed) {
-                    snprintf(buf, sizeof buf, "if ((F & 0x%xu) == 0x%xu) { ", t.fneed, t.fneed);
-                    body = std::string(buf) + body + " }";
-                }
-            }
-            if (co) {
-                snprintf(buf, sizeof buf, "if ((base & 0x%xu) == 0x%xu) { ", co, co);
-                body = std::string(buf) + body + " }";
-            }
-            s += "    " + body + "\n";
+            // (state indices fit 32 bits in the forward sweeps: at most 32 qubits)
+            s += "    " + outer_guard(t, gate_stmt(t, "v", constants_of(t, i).c_str()), false) + "\n";
         }
         g0 = g1;
     }
@@ -334,6 +356,81 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
              "kbwg_jit_sweep(%s::Mem *__restrict__ st, const __grid_constant__ SweepParams p) {\n"
              "  jit::sweep<%s, %d, %d, Body>(st, p);\n}\n",
              geo.threads, geo.ctas_per_sm, geo.policy, geo.policy, geo.K, geo.R);
+    s += buf;
+    return s;
+}
+
+std::string jit_adjoint_source(const JitGeometry &geo, const PlannedSweep &sw, const std::vector<uint32_t> &ginfo) {
+    std::string s;
+    s.reserve(4096 + 320 * sw.gates.size());
+    char buf[512];
+    const int first = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.front();
+    const int last = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.back();
+    s += "#include \"adjoint_dev.cuh\"\n"
+         "using namespace kbwg;\n"
+         "namespace {\n"
+         "struct Body {\n";
+    s += "  static constexpr int kFirst = " + std::to_string(first) + ", kLast = " + std::to_string(last) + ";\n";
+    s += "  template <class P, int K, int R>\n"
+         "  static __device__ __forceinline__ void run(typename P::Amp (&vp)[1 << R], typename P::Amp (&vl)[1 << R],\n"
+         "      typename P::Amp *tp, typename P::Amp *tl, uint32_t FA, uint32_t FB, uint64_t base,\n"
+         "      const TileGate *sg, typename Grad<P>::Wacc *acc) {\n"
+         "    using G = Grad<P>;\n"
+         "    const typename P::K4 kz{};\n";
+    s += std::string("    uint32_t F = ") + (first == LAYOUT_A ? "FA" : "FB") + ";\n";
+    s += "    (void)tp; (void)tl; (void)base; (void)sg; (void)kz; (void)F; (void)acc;\n";
+    static const char *kGradName[] = {"GT_NONE", "GT_X", "GT_Y", "GT_Z", "GT_P1"};
+    int layout = first;
+    size_t g0 = 0;
+    for (size_t st = 0; st < sw.stage_layout.size(); st++) {
+        const int nl = sw.stage_layout[st];
+        if (nl != layout) {
+            snprintf(buf, sizeof buf, "    jit::relayout2<P, K, R, %d, %d>(vp, vl, tp, tl, FA, FB); F = %s;\n", layout,
+                     nl, nl == LAYOUT_A ? "FA" : "FB");
+            s += buf;
+            layout = nl;
+        }
+        const size_t g1 = sw.stage_end[st];
+        for (size_t i = g0; i < g1; i++) {
+            const TileGate &t = sw.gates[i];
+            const int gt = (int)(ginfo[i] & 15u);
+            const unsigned slot = ginfo[i] >> 4;
+            std::string body;
+            if (gt != GT_NONE) {
+                const char *gn = kGradName[gt];
+                std::string expr;
+                if (gt == GT_Z || gt == GT_P1) {
+                    if (t.op >= OP_DREG && t.op < OP_DFIX)
+                        snprintf(buf, sizeof buf, "jit::grad_dreg<P, R, %s, %d, 0x%xu>(vp, vl)", gn, (int)t.rb, t.creg);
+                    else
+                        snprintf(buf, sizeof buf, "jit::grad_dfix<P, R, %s, 0x%xu>(vp, vl, %s)", gn, t.creg,
+                                 side_of(t).c_str());
+                    expr = "if (" + fok_of(t) + ") part = " + std::string(buf) + ";";
+                } else if (t.op < OP_REG) {
+                    snprintf(buf, sizeof buf, "part = jit::grad_lane<P, R, %s, %d, 0x%xu>(vp, vl, %s, F);", gn,
+                             (int)t.tb, t.creg, fok_of(t).c_str());
+                    expr = buf;
+                } else {
+                    snprintf(buf, sizeof buf, "jit::grad_reg<P, R, %s, %d, 0x%xu>(vp, vl)", gn, (int)t.rb, t.creg);
+                    expr = "if (" + fok_of(t) + ") part = " + std::string(buf) + ";";
+                }
+                snprintf(buf, sizeof buf, " jit::grad_store<P, %u>(acc, part);", slot);
+                body += "{ typename G::Acc part = G::zero(); " + expr + buf + " } ";
+            }
+            const std::string k = constants_of(t, i);
+            if (k != "kz") body += "const typename P::K4 k = " + k + "; ";
+            const char *kv = (k != "kz") ? "k" : "kz";
+            body += gate_stmt(t, "vp", kv) + " " + gate_stmt(t, "vl", kv);
+            s += "    " + outer_guard(t, "{ " + body + " }", true) + "\n";
+        }
+        g0 = g1;
+    }
+    s += "  }\n};\n}  // namespace\n";
+    snprintf(buf, sizeof buf,
+             "extern \"C\" __global__ void __launch_bounds__(%d, %d)\n"
+             "kbwg_jit_adjoint(%s::Mem *__restrict__ phi, %s::Mem *__restrict__ lam, const __grid_constant__ AdjParams a) {\n"
+             "  jit::adjoint_sweep<%s, %d, %d, Body>(phi, lam, a);\n}\n",
+             geo.threads, geo.ctas_per_sm, geo.policy, geo.policy, geo.policy, geo.K, geo.R);
     s += buf;
     return s;
 }

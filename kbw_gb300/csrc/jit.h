@@ -23,6 +23,11 @@ struct JitGeometry {
 // launched like k_sweep with (Mem *state, SweepParams)).
 std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw);
 
+// Source of the specialised reverse (adjoint) sweep of `sw` (entry point
+// kbwg_jit_adjoint, launched like k_adjoint with (phi, lambda, AdjParams));
+// ginfo per gate of the sweep: gradient type | slot << 4.
+std::string jit_adjoint_source(const JitGeometry &geo, const PlannedSweep &sw, const std::vector<uint32_t> &ginfo);
+
 // Compiled kernels for the sweeps of a plan, one entry per sweep (nullptr
 // where none could be built).  Sources already compiled in this process are
 // reused; the others are compiled in parallel.  Returns false if NVRTC is

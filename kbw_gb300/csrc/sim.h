@@ -107,6 +107,12 @@ cudaError_t flush_queue(Sim &s);
 // Fusion planner entry used by flush_queue (sweep.cu).
 cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
 
+// Specialised kernels (entry point `entry`) for complete sources, following
+// the handle's JIT mode: always: compiled now; auto: from the second request
+// of the same sources on, compiled in the background, loaded once done (null
+// entries until then); off: none.
+std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry);
+
 // Wait for the handle's background compilations of specialised kernels;
 // true if any was still to be used (a later flush of its structure loads it).
 bool wait_specialised(Sim &s);
@@ -115,6 +121,11 @@ bool wait_specialised(Sim &s);
 // kernel of every sweep a flush of `gates` would run on `s`; returns the
 // number of failed compilations and sets `sweeps`.
 size_t jit_check(const Sim &s, const GateDesc *gates, size_t count, size_t &sweeps);
+
+// The same for the reverse sweeps of an adjoint gradient of `fwd` (gtype:
+// GT_* per gate), one segment.
+size_t jit_check_adjoint(const Sim &s, const std::vector<GateDesc> &fwd, const std::vector<int> &gtype,
+                         size_t &sweeps);
 
 // Tile sizes K (2^K amplitudes per tile) with a compiled sweep kernel for
 // the handle's arithmetic and qubit count, the default first; empty when the
@@ -138,8 +149,6 @@ struct PauliString {
     double coef = 0.0;
 };
 
-// Gradient types of the adjoint sweep.
-enum { GT_NONE = 0, GT_X = 1, GT_Y = 2, GT_Z = 3, GT_P1 = 4 };
 
 // Batched hardware-efficient-ansatz circuits with ring-TFIM energies (hea.cu).
 int32_t hea_batch(int precision, bool fast_c128, size_t ncirc, const uint32_t *num_qubits, const uint32_t *layers,

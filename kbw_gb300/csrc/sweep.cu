@@ -616,6 +616,44 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
     return out;
 }
 
+std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry) {
+    std::vector<const void *> out(srcs.size(), nullptr);
+    if (s.jit_mode == KBWG_JIT_OFF || srcs.empty()) return out;
+    if (s.jit_mode == KBWG_JIT_AUTO && s.n < jit_min_qubits()) return out;
+    if (s.jit_mode == KBWG_JIT_AUTO) {
+        if (!s.graphs) s.graphs = new GraphCache();
+        GraphCache &gc = *(GraphCache *)s.graphs;
+        uint64_t h = 1469598103934665603ull;  // FNV-1a over the sources
+        for (const std::string &src : srcs)
+            for (unsigned char c : src) {
+                h ^= c;
+                h *= 1099511628211ull;
+            }
+        SpecialisedJob *job = nullptr;
+        for (SpecialisedJob &j : gc.jobs)
+            if (j.key == h) job = &j;
+        if (!job) {
+            bool repeat = false;
+            for (uint64_t x : gc.seen) repeat = repeat || x == h;
+            if (!repeat) {  // first sight: remember it
+                if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
+                gc.seen.push_back(h);
+                return out;
+            }
+            if (gc.jobs.size() >= kJobEntries) gc.jobs.erase(gc.jobs.begin());
+            SpecialisedJob nj;
+            nj.key = h;
+            nj.job = jit_prefetch(srcs);
+            gc.jobs.push_back(nj);
+            return out;
+        }
+        if (!jit_job_done(*job->job)) return out;
+        job->used = true;
+    }
+    for (size_t i = 0; i < srcs.size(); i++) out[i] = jit_kernel(srcs[i], entry);
+    return out;
+}
+
 bool wait_specialised(Sim &s) {
     GraphCache *gc = (GraphCache *)s.graphs;
     if (!gc) return false;

@@ -95,6 +95,10 @@ __host__ __device__ inline void tile_gate_dispatch(TileGate &g, int R0, int R) {
     else g.op = OP_DFIX + (g.cls - TG_Z);
 }
 
+// Gradient types of the adjoint sweep: the generator of a differentiated
+// gate (RX: X, RY: Y, RZ: Z, P: the |1> projector).
+enum { GT_NONE = 0, GT_X = 1, GT_Y = 2, GT_Z = 3, GT_P1 = 4 };
+
 // Layout A holds local bits [5, 5+R) in registers, layout B [K-R, K).
 enum { LAYOUT_A = 0, LAYOUT_B = 1 };
 

@@ -210,3 +210,21 @@ def test_planner_long_lists_and_stage_limit(lib, prec):
     ref.apply(circ)
     tol = 1e-12 if prec == "c128" else 1e-4
     assert rel_err(o.state(), ref.state()) < tol
+
+
+@pytest.mark.parametrize("prec,flags", [(N.C64, 0), (N.C128, N.FLAG_FAST_C128), (N.C128, 0)])
+def test_specialised_adjoint_kernels_compile(lib, prec, flags):
+    """The specialised reverse sweeps of the adjoint gradient compile for
+    every arithmetic (host only): a hardware-efficient ansatz and a random
+    circuit with controlled parameterised gates."""
+    from kbw_gb300.dense import _gate_array
+    n = 14
+    circ = C.hea(n, 2, C.hea_params(n, 2, 3)) + C.random_circuit(n, 60, 9, max_controls=2)
+    try:
+        sweeps, failed = N.jit_check_adjoint(n, prec, flags, _gate_array(circ))
+    except N.KbwgError as e:
+        if e.code == N.EUNSUPPORTED:
+            pytest.skip("NVRTC not available: %s" % e)
+        raise
+    assert sweeps > 0
+    assert failed == 0, N.jit_last_error()

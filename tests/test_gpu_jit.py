@@ -135,3 +135,32 @@ def test_auto_mode_skips_small_registers():
         sim.apply(circ)
         sim.flush()
         assert sim.jit_info()["last_specialised"] == 0
+
+
+@pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", True), ("c128", False)])
+def test_specialised_adjoint_equals_interpreted(prec, fast):
+    # a hardware-efficient ansatz plus controlled rotations and phases (the
+    # gradient's control projector on lane, register and outer bits), two
+    # checkpoint segments
+    n, L = 16, 3
+    params = C.hea_params(n, L, 4)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    extra = C.random_circuit(n, 80, 12, max_controls=2, kinds=[C.RX, C.RY, C.RZ, C.P, C.H, C.X])
+    k = len(params)
+    for g in extra:
+        circ.append(g)
+        if g[0] in C.PARAMETRIC:
+            pidx.append(k)
+            k += 1
+        else:
+            pidx.append(-1)
+    ham = C.tfim_ring(n)
+    res = []
+    for jit in (N.JIT_OFF, N.JIT_ALWAYS):
+        sim = DenseGB300(n, prec, fast_c128=fast, jit=jit)
+        res.append(sim.adjoint_gradient(circ, pidx, k, ham, max_checkpoints=1))
+        sim.close()
+    assert res[0][0] == res[1][0]
+    assert np.array_equal(res[0][1], res[1][1])
+    assert N.jit_info()["failed"] == 0, N.jit_last_error()
