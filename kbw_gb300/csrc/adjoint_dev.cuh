@@ -24,18 +24,22 @@ struct Grad<Fast<T>> {
     using Amp = cx<T>;
     using Acc = T;
     static __device__ __forceinline__ Acc zero() { return (T)0; }
+    // (each product and sum rounded on its own: a contracted form would depend
+    // on how the compiler fuses the surrounding code)
+    static __device__ __forceinline__ T im_conj(Amp l, Amp b) { return xsub(xmul(l.re, b.im), xmul(l.im, b.re)); }
+    static __device__ __forceinline__ T re_conj(Amp l, Amp b) { return xadd(xmul(l.re, b.re), xmul(l.im, b.im)); }
     static __device__ __forceinline__ Acc term(int gt, bool one, Amp l, Amp p, Amp pp) {
         switch (gt) {
-        case GT_X: return l.re * pp.im - l.im * pp.re;
+        case GT_X: return im_conj(l, pp);
         case GT_Y: {
-            const T r = l.re * pp.re + l.im * pp.im;
+            const T r = re_conj(l, pp);
             return one ? r : -r;
         }
         case GT_Z: {
-            const T r = l.re * p.im - l.im * p.re;
+            const T r = im_conj(l, p);
             return one ? -r : r;
         }
-        default: return one ? (T)-2 * (l.re * p.im - l.im * p.re) : (T)0;
+        default: return one ? (T)-2 * im_conj(l, p) : (T)0;
         }
     }
     static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
