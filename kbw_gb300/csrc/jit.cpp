@@ -551,6 +551,8 @@ void run_job(std::shared_ptr<JitJob> job) {
         false);
     {
         std::lock_guard<std::mutex> lk(job->mu);
+        job->srcs.clear();  // the cubins are in the cache; the sources are no longer needed
+        job->srcs.shrink_to_fit();
         job->done = true;
     }
     job->cv.notify_all();

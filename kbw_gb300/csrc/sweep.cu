@@ -205,7 +205,10 @@ struct GraphCache {
     std::vector<SpecialisedJob> jobs;
     uint64_t clock = 0;
 };
-constexpr size_t kJobEntries = 32;
+// (an adjoint gradient alone brings two structures per checkpoint segment:
+// its forward and its reverse sweeps)
+constexpr size_t kJobEntries = 128;
+constexpr size_t kSeenEntries = 256;
 constexpr size_t kGraphCacheEntries = 8;
 
 static void free_entry(SweepGraph &g) {
@@ -289,7 +292,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
         h = hash_of(sig);
         for (uint64_t x : gc.seen) repeat = repeat || x == h;
         if (!repeat) {  // first sight of this structure: launch directly, remember it
-            if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
+            if (gc.seen.size() >= kSeenEntries) gc.seen.erase(gc.seen.begin());
             gc.seen.push_back(h);
         }
         if (auto_jit)
@@ -636,7 +639,7 @@ std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::str
             bool repeat = false;
             for (uint64_t x : gc.seen) repeat = repeat || x == h;
             if (!repeat) {  // first sight: remember it
-                if (gc.seen.size() >= 4 * kGraphCacheEntries) gc.seen.erase(gc.seen.begin());
+                if (gc.seen.size() >= kSeenEntries) gc.seen.erase(gc.seen.begin());
                 gc.seen.push_back(h);
                 return out;
             }
