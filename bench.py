@@ -244,7 +244,7 @@ def single_gate_sweep(sim, torch, peak, C, reps=5):
             "avg_launch_ms": round(kms / max(nl, 1), 4), "launches": nl}
 
 
-def run_adjoint_bench(args, torch, DenseGB300, C):
+def run_adjoint_bench(args, torch, DenseGB300, C, grads):
     """Gradient half of the metric: 24 qubits, 10 layers of RY, RZ on every
     qubit + CZ ring (480 parameters), ring TFIM.  grads/s of the adjoint
     kernel vs the parameter-shift rule on the same GPU, plus the max
@@ -295,6 +295,7 @@ def run_adjoint_bench(args, torch, DenseGB300, C):
                          "speedup_adjoint_vs_param_shift": round(tp / ta, 1),
                          "max_grad_err_vs_param_shift": float(np.max(np.abs(g - g_ps)))})
         out[label] = item
+        grads[label] = g
         sim.close()
     return out
 
@@ -447,6 +448,158 @@ def run_batch_bench(args, torch, C):
             "config": "hea-batch n~U{8..20} L~U{2..8} ring-TFIM, one persistent launch (incl. host<->device copies)"}
 
 
+# ---- parity against the oracle at the benchmark's own sizes ----------------------------
+# The oracle (oracle/, a C restatement of kbw Dense<f64>) is the checker here,
+# run on the host beside the GPU work and never timed: the 30-qubit brickwork
+# state, its <Z_q> and one full measurement with injected draws, and
+# parameter-shift gradients of the 24-qubit ansatz at a spread of parameters.
+PARITY_PARAMS = 24
+
+
+def parity_param_picks(n, layers, count=PARITY_PARAMS):
+    """`count` parameters of the hardware-efficient ansatz spread over every
+    layer, alternating RY and RZ, on varying qubits."""
+    picks = set()
+    for j in range(count):
+        layer = (j * layers) // count
+        picks.add(layer * 2 * n + (j % 2) * n + (7 * j) % n)
+    return sorted(picks)
+
+
+class OracleParity(threading.Thread):
+    def __init__(self, args, C, circ30, n30):
+        super().__init__(daemon=True)
+        self.args, self.C, self.circ30, self.n30 = args, C, circ30, n30
+        self.result = {}
+        self.error = None
+
+    def run(self):
+        try:
+            import oracle
+            oracle.set_num_threads(max(1, (os.cpu_count() or 4) - 2))  # two cores stay with the GPU host work
+            C = self.C
+            t0 = time.perf_counter()
+            # 24-qubit gradient: oracle parameter shift at the picked parameters
+            n, L = self.args.adj_qubits, self.args.adj_layers
+            params = C.hea_params(n, L, 0)
+            circ = C.hea(n, L, params)
+            pidx = C.hea_param_index(n, L)
+            ham = C.tfim_ring(n)
+            gate_of = {p: i for i, p in enumerate(pidx) if p >= 0}
+            picks = parity_param_picks(n, L)
+            o = oracle.OracleDense(n, "c128")
+            done = 0  # o holds circ[:done]
+            ps = []
+            for k in picks:
+                g = gate_of[k]
+                o.apply(circ[done:g])
+                done = g
+                base = o.state()
+                kind, t, c, a = circ[g]
+                ev = []
+                for d in (math.pi / 2, -math.pi / 2):
+                    o.set_state(base)
+                    o.apply([(kind, t, c, a + d)] + circ[g + 1:])
+                    ev.append(o.pauli_expect(ham))
+                ps.append((ev[0] - ev[1]) / 2)
+                o.set_state(base)
+            del o
+            self.result["grad"] = {"picks": picks, "param_shift": ps, "seconds": time.perf_counter() - t0}
+            # 30-qubit brickwork from |0>
+            t0 = time.perf_counter()
+            n = self.n30
+            o = oracle.OracleDense(n, "c128")
+            o.apply(self.circ30)
+            self.result["z"] = o.z_all()
+            self.result["state"] = o.state()
+            draws = C.uniform_draws(n, 7)
+            self.result["bits"] = o.measure(list(range(n)), draws)
+            self.result["draws"] = draws
+            self.result["seconds30"] = time.perf_counter() - t0
+            del o
+        except Exception as e:  # reported in the bench line
+            self.error = repr(e)
+
+
+def parity_report(chk, args, torch, DenseGB300, C, circ30, n30, grads):
+    """GPU side of the parity checks, after the timed work: the oracle's
+    30-qubit state is uploaded to a handle and compared on the device."""
+    if chk is None:
+        return None
+    chk.join()
+    import oracle
+    oracle.set_num_threads(os.cpu_count() or 1)
+    if chk.error:
+        return {"error": chk.error}
+    r = chk.result
+    out = {"checker": "oracle (restated Dense<f64>, OpenMP, %d threads)" % max(1, (os.cpu_count() or 4) - 2)}
+    # ---- 30-qubit brickwork ----
+    ref = DenseGB300(n30, "c128")
+    ref.set_state(r.pop("state"))
+    ff = DenseGB300(n30, "c128", fast_c128=True)
+    ff.apply(circ30)
+    s64 = DenseGB300(n30, "c64")
+    s64.apply(circ30)
+    zs = [[(1.0, [(C.PAULI_Z, q)])] for q in range(n30)]
+    z_ff = np.array([ff.exp_value(h) for h in zs])
+    z_64 = np.array([s64.exp_value(h) for h in zs])
+    bits_ff = ff.measure(list(range(n30)), r["draws"])
+    bits_64 = s64.measure(list(range(n30)), r["draws"])
+    ff.close()
+    s64.close()
+    ff = DenseGB300(n30, "c128", fast_c128=True)
+    ff.apply(circ30)
+    rel = ff.distance(ref)
+    ff.close()
+    s64 = DenseGB300(n30, "c64")
+    s64.apply(circ30)
+    infid = 1.0 - s64.fidelity(ref)
+    s64.close()
+    ref.close()
+    out["brickwork_30q"] = {
+        "float_float_relative_l2": rel, "c64_infidelity": infid,
+        "max_abs_dZ_float_float": float(np.max(np.abs(z_ff - r["z"]))),
+        "max_abs_dZ_c64": float(np.max(np.abs(z_64 - r["z"]))),
+        "measurement_equal_float_float": bits_ff == r["bits"], "measurement_equal_c64": bits_64 == r["bits"],
+        "oracle_seconds": round(r["seconds30"], 1),
+        "bar": "relative L2 <= 1e-12 (complex128); outcomes equal for the same draws"}
+    # ---- 24-qubit gradient ----
+    g = r["grad"]
+    picks = g["picks"]
+    ps = np.array(g["param_shift"])
+    n, L = args.adj_qubits, args.adj_layers
+    params = C.hea_params(n, L, 0)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    # central differences, h = 1e-6, on the engine's order-preserving binary64
+    # path (the restated Dense<f64> arithmetic, bit for bit)
+    h = 1e-6
+    ex = DenseGB300(n, "c128", exact_order=True)
+    fd = []
+    for k in picks:
+        ev = []
+        for d in (h, -h):
+            p2 = params.copy()
+            p2[k] += d
+            ex.clear()
+            ex.apply(C.hea(n, L, p2))
+            ev.append(ex.exp_value(ham))
+        fd.append((ev[0] - ev[1]) / (2 * h))
+    ex.close()
+    fd = np.array(fd)
+    item = {"params_checked": len(picks), "layers_covered": len({k // (2 * n) for k in picks}),
+            "oracle_param_shift_seconds": round(g["seconds"], 1),
+            "fd_h": h, "max_abs_ps_minus_fd": float(np.max(np.abs(ps - fd)))}
+    for label, gv in grads.items():
+        gs = np.asarray(gv)[picks]
+        item[label] = {"max_abs_err_vs_oracle_param_shift": float(np.max(np.abs(gs - ps))),
+                       "max_abs_err_vs_central_fd": float(np.max(np.abs(gs - fd)))}
+    item["bar"] = "<= 1e-10 (complex128), <= 1e-5 (complex64)"
+    out["adjoint_24q"] = item
+    return out
+
+
+
 def rounded(d, digits=3):
     return {k: round(v, digits) if isinstance(v, float) else v for k, v in d.items()}
 
@@ -468,6 +621,21 @@ def run_ours(args, world, rank, local):
     G = len(circ)
     step_bytes = G * 2 * B * (1 << n)
     peak, peak_kind = load_peaks()
+
+    # CPU baseline first, on an idle host; then the oracle checker starts
+    # beside the GPU work (it never overlaps a CPU timing)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, info = cpu_port_rate(n, prec, circ, args.cpu_seconds)
+        if rate is not None:
+            cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": info.get("threads"), "kind": "port",
+                   "sample": "first %d gates of the %dq brickwork on the restated Dense<%s> (OpenMP), %.1f s"
+                             % (info["gates"], info["qubits"], "f64" if prec == "c128" else "f32", info["seconds"])}
+    checker = None
+    adj_grads = {}
+    if rank == 0 and world == 1 and args.parity and prec == "c128" and fast:
+        checker = OracleParity(args, C, circ, n)
+        checker.start()
 
     sim = DenseGB300(n, prec, fast_c128=fast)
     ext = torch.cuda.ExternalStream(sim.stream_handle())
@@ -606,21 +774,17 @@ def run_ours(args, world, rank, local):
         sim.close()
 
     if args.adjoint:
-        secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C)
+        secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C, adj_grads)
     if args.adjoint_large:
         secondary["adjoint_large"] = run_adjoint_large(args, torch, DenseGB300, C)
+    # (joined before the batch and Grover items, which run the oracle on the host)
+    if checker is not None:
+        secondary["parity_vs_oracle"] = parity_report(checker, args, torch, DenseGB300, C, circ, n, adj_grads)
     if args.batch:
         secondary["batch"] = run_batch_bench(args, torch, C)
     if args.grover:
         secondary["grover"] = run_grover_bench(args, torch, DenseGB300, C)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        rate, info = cpu_port_rate(n, prec, circ, args.cpu_seconds)
-        if rate is not None:
-            cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": info.get("threads"), "kind": "port",
-                   "sample": "first %d gates of the %dq brickwork on the restated Dense<%s> (OpenMP), %.1f s"
-                             % (info["gates"], info["qubits"], "f64" if prec == "c128" else "f32", info["seconds"])}
 
     if rank == 0:
         line = {
@@ -655,6 +819,8 @@ def main():
                     help="complex128 gate arithmetic: float-float (default) or IEEE binary64")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the oracle parity checks at the benchmark sizes (30q state, 24q gradients)")
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="keep the default tile size and fusion depth instead of autotuning them")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

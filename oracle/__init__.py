@@ -52,6 +52,9 @@ def lib():
         L.od_sample.argtypes = [ctypes.c_void_p, szp, sz, sz, dp, u64p, u64p]
         L.od_exp_value.restype = ctypes.c_double
         L.od_exp_value.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), szp, szp, dp, sz]
+        L.od_pauli_expect.restype = ctypes.c_double
+        L.od_pauli_expect.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), szp, szp, dp, sz]
+        L.od_z_all.argtypes = [ctypes.c_void_p, dp]
         L.od_get_state.argtypes = [ctypes.c_void_p, dp]
         L.od_set_state.argtypes = [ctypes.c_void_p, dp]
         L.od_swap_qubits.argtypes = [ctypes.c_void_p, sz, sz]
@@ -163,6 +166,14 @@ class OracleDense:
 
     def exp_value(self, hamiltonian):
         """hamiltonian: list of (coefficient, [(pauli_code, qubit), ...])."""
+        return self._expect(lib().od_exp_value, hamiltonian)
+
+    def pauli_expect(self, hamiltonian):
+        """<H> from the amplitudes directly (parity checks needing many
+        energies); equals exp_value up to the dump's epsilon filter."""
+        return self._expect(lib().od_pauli_expect, hamiltonian)
+
+    def _expect(self, fn, hamiltonian):
         paulis, qubits, offsets, coefs = [], [], [0], []
         for coef, terms in hamiltonian:
             for p, q in terms:
@@ -174,8 +185,14 @@ class OracleDense:
         qa = np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp)
         oa = np.ascontiguousarray(offsets, dtype=np.uintp)
         ca = np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64)
-        return lib().od_exp_value(self._h, _ptr(pa, ctypes.c_int), _ptr(qa, ctypes.c_size_t),
-                                  _ptr(oa, ctypes.c_size_t), _ptr(ca, ctypes.c_double), len(coefs))
+        return fn(self._h, _ptr(pa, ctypes.c_int), _ptr(qa, ctypes.c_size_t), _ptr(oa, ctypes.c_size_t),
+                  _ptr(ca, ctypes.c_double), len(coefs))
+
+    def z_all(self):
+        """<Z_q> for every qubit (one pass over the state)."""
+        out = np.zeros(self.num_qubits, np.float64)
+        lib().od_z_all(self._h, _ptr(out, ctypes.c_double))
+        return out
 
     # -- raw access ------------------------------------------------------------
     def state(self):

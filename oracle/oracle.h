@@ -80,6 +80,14 @@ long od_sample(od_state *s, const size_t *qubits, size_t n_qubits, size_t shots,
 double od_exp_value(od_state *s, const int *paulis, const size_t *qubits, const size_t *offsets,
                     const double *coefficients, size_t n_strings);
 
+/* <H> from the amplitudes directly (no basis rotations, no dump): for
+ * parity checks that need many energies.  Same arguments as od_exp_value. */
+double od_pauli_expect(const od_state *s, const int *paulis, const size_t *qubits, const size_t *offsets,
+                       const double *coefficients, size_t n_strings);
+
+/* <Z_q> of every qubit in one pass over the state (out: num_qubits entries). */
+void od_z_all(const od_state *s, double *out);
+
 /* Raw state access (interleaved re,im as double). */
 void od_get_state(const od_state *s, double *out);
 void od_set_state(od_state *s, const double *in);

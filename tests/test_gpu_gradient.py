@@ -123,3 +123,57 @@ def test_torch_autograd_bridge():
     e.backward()
     want = oracle_param_shift(n, C.hea(n, L, params.detach().numpy()), pidx, params.numel(), ham)
     assert np.max(np.abs(params.grad.numpy() - want)) < 1e-10
+
+
+def test_adjoint_24q_slice_vs_oracle_param_shift_and_fd():
+    """The gradient configuration's register size (24 qubits; two of its ten
+    layers): adjoint gradients in all three arithmetics at parameters of both
+    layers and both rotation kinds, against parameter shift on the oracle
+    (energies from its amplitudes) and central differences with h = 1e-6 on
+    the engine's order-preserving binary64 path (the Dense<f64> arithmetic)."""
+    n, L = 24, 2
+    params = C.hea_params(n, L, 5)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    ham = C.tfim_ring(n)
+    picks = [0, 7, 29, 47, 50, 71, 88, 95]  # layer 0/1 x RY/RZ
+    gate_of = {p: i for i, p in enumerate(pidx) if p >= 0}
+    o = oracle.OracleDense(n, "c128")
+    done, ps = 0, []
+    for k in picks:
+        g = gate_of[k]
+        o.apply(circ[done:g])
+        done = g
+        base = o.state()
+        kind, t, c, a = circ[g]
+        ev = []
+        for d in (math.pi / 2, -math.pi / 2):
+            o.set_state(base)
+            o.apply([(kind, t, c, a + d)] + circ[g + 1:])
+            ev.append(o.pauli_expect(ham))
+        ps.append(0.5 * (ev[0] - ev[1]))
+        o.set_state(base)
+    ps = np.array(ps)
+    h = 1e-6
+    ex = DenseGB300(n, "c128", exact_order=True)
+    fd = []
+    for k in picks:
+        ev = []
+        for d in (h, -h):
+            p2 = params.copy()
+            p2[k] += d
+            ex.clear()
+            ex.apply(C.hea(n, L, p2))
+            ev.append(ex.exp_value(ham))
+        fd.append((ev[0] - ev[1]) / (2 * h))
+    fd = np.array(fd)
+    # the finite differences themselves carry ~1e-10 of rounding (eps / h)
+    assert np.max(np.abs(ps - fd)) < 1e-8
+    for prec, fast, tol, tol_fd in (("c128", True, 1e-10, 1e-8), ("c128", False, 1e-10, 1e-8),
+                                    ("c64", False, 1e-5, 1e-5)):
+        sim = DenseGB300(n, prec, fast_c128=fast)
+        _, grad = sim.adjoint_gradient(circ, pidx, len(params), ham)
+        sim.close()
+        gs = grad[picks]
+        assert np.max(np.abs(gs - ps)) < tol, (prec, fast, np.max(np.abs(gs - ps)))
+        assert np.max(np.abs(gs - fd)) < tol_fd, (prec, fast, np.max(np.abs(gs - fd)))
