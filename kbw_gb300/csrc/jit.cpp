@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -522,6 +523,21 @@ struct Runner {
 };
 Runner g_runner;
 
+// Stop the background jobs between compilations and join them.  Registered
+// with atexit on the first submission, after NVRTC has been opened: exit
+// handlers run in reverse order of registration, so this one runs before
+// NVRTC's own teardown (a job still inside NVRTC then would crash the exit).
+void stop_jobs() {
+    g_runner.stop = true;
+    std::vector<std::thread> ts;
+    {
+        std::lock_guard<std::mutex> lk(g_runner.mu);
+        for (auto &t : g_runner.threads)
+            if (t.first.joinable()) ts.push_back(std::move(t.first));
+    }
+    for (std::thread &t : ts) t.join();
+}
+
 void run_job(std::shared_ptr<JitJob> job) {
     std::vector<size_t> todo;
     {
@@ -567,6 +583,8 @@ std::shared_ptr<JitJob> jit_prefetch(std::vector<std::string> srcs) {
         job->done = true;
         return job;
     }
+    static std::once_flag registered;
+    std::call_once(registered, [] { std::atexit(stop_jobs); });
     std::lock_guard<std::mutex> lk(g_runner.mu);
     // join the workers of finished jobs
     for (size_t i = 0; i < g_runner.threads.size();) {
