@@ -406,6 +406,14 @@ int32_t kbwg_set_jit(kbwg_sim *sim, int32_t mode);
  * each of those structures runs specialised (e.g. before a timed region). */
 int32_t kbwg_jit_wait(kbwg_sim *sim);
 
+/* Stop background compilation for the rest of the process and wait for the
+ * compilations in progress (each finishes; none starts).  Call it before the
+ * process exits if flushes may have started compilations: a compilation
+ * still running while the process tears down its libraries can crash the
+ * exit.  (The Python binding registers it to run at interpreter exit.)
+ * Later flushes run the kernels already compiled and the interpreted ones. */
+int32_t kbwg_jit_shutdown(void);
+
 typedef struct kbwg_jit_stats {
     int32_t mode;                /* the handle's KBWG_JIT_* mode */
     int32_t available;           /* 1 if NVRTC could be opened */

@@ -4,6 +4,7 @@ The library is built in-tree by ``kbw_gb300/build.py`` (or
 ``__graft_entry__.build()``).  Loading fails loudly when it is missing: there
 is no CPU fallback.
 """
+import atexit
 import ctypes
 import os
 
@@ -111,6 +112,7 @@ SIGNATURES = {
     "kbwg_autotune": (_I32, [_P, ctypes.POINTER(Gate), _U, ctypes.c_uint32, ctypes.c_void_p]),
     "kbwg_set_jit": (_I32, [_P, _I32]),
     "kbwg_jit_wait": (_I32, [_P]),
+    "kbwg_jit_shutdown": (_I32, []),
     "kbwg_jit_info": (_I32, [_P, ctypes.c_void_p]),
     "kbwg_jit_last_error": (ctypes.c_char_p, []),
     "kbwg_jit_check": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,
@@ -139,6 +141,8 @@ def load(path=None):
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    # background compilations must end before the C library teardown
+    atexit.register(lib.kbwg_jit_shutdown)
     return lib
 
 

@@ -1408,6 +1408,13 @@ int32_t kbwg_jit_wait(kbwg_sim *s) {
     GUARD_END
 }
 
+int32_t kbwg_jit_shutdown(void) {
+    GUARD_BEGIN
+    jit_shutdown();
+    return KBWG_OK;
+    GUARD_END
+}
+
 int32_t kbwg_jit_info(kbwg_sim *s, kbwg_jit_stats *out) {
     GUARD_BEGIN
     if (!out) return fail(KBWG_EINVAL, "null argument");

@@ -523,10 +523,13 @@ struct Runner {
 };
 Runner g_runner;
 
-// Stop the background jobs between compilations and join them.  Registered
-// with atexit on the first submission, after NVRTC has been opened: exit
-// handlers run in reverse order of registration, so this one runs before
-// NVRTC's own teardown (a job still inside NVRTC then would crash the exit).
+// Stop the background jobs between compilations and join them.  A job still
+// inside NVRTC when the process runs its exit handlers would crash the exit:
+// NVRTC registers its own teardown lazily, during its first compilations, so
+// it can run before any handler registered earlier.  Callers therefore stop
+// the jobs before exit (kbwg_jit_shutdown; the Python binding registers it
+// with Python's atexit, which runs before the C exit handlers); the atexit
+// registration below is a best effort for hosts that do not.
 void stop_jobs() {
     g_runner.stop = true;
     std::vector<std::thread> ts;
@@ -575,9 +578,15 @@ void run_job(std::shared_ptr<JitJob> job) {
 }
 }  // namespace
 
+void jit_shutdown() { stop_jobs(); }
+
 std::shared_ptr<JitJob> jit_prefetch(std::vector<std::string> srcs) {
     auto job = std::make_shared<JitJob>();
     job->srcs = std::move(srcs);
+    if (g_runner.stop) {  // shut down: nothing more is compiled in the background
+        job->done = true;
+        return job;
+    }
     if (!jit_available()) {
         note_error(nvrtc().why);
         job->done = true;

@@ -49,6 +49,9 @@ size_t jit_compile_only(const std::vector<std::string> &srcs);
 struct JitJob;
 std::shared_ptr<JitJob> jit_prefetch(std::vector<std::string> srcs);
 bool jit_job_done(const JitJob &job);
+// Stop background compilation for good (between compilations) and wait for
+// the jobs; later jobs complete at once without compiling.
+void jit_shutdown();
 void jit_job_wait(JitJob &job);
 
 bool jit_available();

@@ -168,19 +168,21 @@ def test_specialised_adjoint_equals_interpreted(prec, fast):
 
 def test_exit_while_compiling_in_background():
     # the second flush starts a background compilation; the process exits
-    # at once, while NVRTC may still be compiling: the exit must be clean
+    # at once, with NVRTC still compiling: the exit must be clean (the
+    # binding stops background compilation before the library teardown)
     import os
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     code = ("import sys; sys.path.insert(0, %r)\n"
             "from kbw_gb300 import DenseGB300, _native as N, circuits as C\n"
-            "s = DenseGB300(20, 'c64', jit=N.JIT_AUTO)\n"
-            "c = C.random_circuit(20, 120, 5, max_controls=1)\n"
+            "s = DenseGB300(21, 'c128', fast_c128=True, jit=N.JIT_AUTO)\n"
+            "c = C.brickwork(21, 6, 2)\n"
             "for _ in range(2):\n"
             "    s.apply(c)\n"
             "    s.flush()\n"
             "print('done')\n" % root)
-    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
-    assert "done" in r.stdout
+    for _ in range(3):
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+        assert "done" in r.stdout
