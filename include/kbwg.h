@@ -123,7 +123,10 @@ int32_t kbwg_measure_collapse(kbwg_sim *sim, uintptr_t target, bool result, doub
 /* QubitManager::do_measure (src/quantum_execution.rs:272-292): measure the
  * listed qubits one at a time, last listed first, with one uniform draw in
  * [0,1) per qubit taken from `draws` in that order (the reference draws
- * these from its StdRng).  draws == NULL uses the handle's own generator
+ * these from its StdRng: pass the UniformFloat<f64> value WeightedIndex
+ * takes from one next_u64, (x >> 12 | 0x3FF0000000000000) as a double
+ * minus 1, not rand's 53-bit StandardUniform).  draws == NULL uses the
+ * handle's own generator (kbwg_draws)
  * (seeded from KBW_SEED).  *result packs qubits[0] as the most significant
  * bit. */
 int32_t kbwg_measure(kbwg_sim *sim, const uintptr_t *qubits, uintptr_t n_qubits,
@@ -281,6 +284,22 @@ int32_t kbwg_plan(uintptr_t num_qubits, int32_t precision, uint32_t flags, const
 int32_t kbwg_plan_tuned(uintptr_t num_qubits, int32_t precision, uint32_t flags, uint32_t tile_qubits,
                         uint32_t fusion_depth, const kbwg_gate *gates, uintptr_t n_gates, uint32_t *order,
                         uint32_t *sweep_end, uint64_t *tile_mask, uintptr_t *n_sweeps);
+
+/* The draws a register takes when the caller passes none: rand's StdRng
+ * (ChaCha12) seeded with StdRng::seed_from_u64(seed), as the reference's
+ * QubitManager seeds it from KBW_SEED (src/quantum_execution.rs:181-191);
+ * each draw is the UniformFloat<f64> sample WeightedIndex consumes, the 52
+ * high bits of one next_u64 as a double in [1, 2) minus 1
+ * (src/convert.rs:60-64).  Writes the first `count` draws of a fresh
+ * generator.  (The crates are not available here: the stream is restated
+ * from their published algorithms, its ChaCha core checked against
+ * RFC 7539.) */
+int32_t kbwg_draws(uint64_t seed, uintptr_t count, double *out);
+
+/* One ChaCha block (diagnostic of the generator above): 8 key words, 64-bit
+ * block counter (state words 12-13), 64-bit stream (words 14-15), an even
+ * number of rounds (12 for StdRng, 20 for RFC 7539); 16 output words. */
+int32_t kbwg_chacha_block(const uint32_t *key, uint64_t counter, uint64_t stream, uint32_t rounds, uint32_t *out);
 
 /* Make `device` current for this library on the calling thread; kbwg_new
  * places new handles on the current device (0 unless selected). */

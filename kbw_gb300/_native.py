@@ -118,6 +118,9 @@ SIGNATURES = {
     "kbwg_jit_check": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Gate), _U,
                               _UP, _UP]),
     "kbwg_jit_check_adjoint": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, _UP, _UP]),
+    "kbwg_draws": (_I32, [ctypes.c_uint64, _U, _DP]),
+    "kbwg_chacha_block": (_I32, [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                 ctypes.POINTER(ctypes.c_uint32)]),
     "kbwg_masked_norm_noalloc": (_I32, [_P, _U, _I32, ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "kbwg_last_error": (ctypes.c_char_p, []),
     "kbwg_launch_count": (ctypes.c_uint64, []),
@@ -198,6 +201,23 @@ def jit_check_adjoint(num_qubits, prec, flags, gates):
     check(load().kbwg_jit_check_adjoint(int(num_qubits), prec, int(flags), gates, len(gates), ctypes.byref(ns),
                                         ctypes.byref(nf)))
     return int(ns.value), int(nf.value)
+
+
+def draws(seed, count):
+    """The first `count` draws of a register's generator seeded with `seed`
+    (rand's StdRng::seed_from_u64 + UniformFloat<f64>)."""
+    import numpy as np
+    out = np.zeros(max(int(count), 1), np.float64)
+    check(load().kbwg_draws(int(seed) & 0xFFFFFFFFFFFFFFFF, int(count),
+                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return out[: int(count)]
+
+
+def chacha_block(key, counter, stream, rounds):
+    k = (ctypes.c_uint32 * 8)(*key)
+    out = (ctypes.c_uint32 * 16)()
+    check(load().kbwg_chacha_block(k, int(counter), int(stream), int(rounds), out))
+    return list(out)
 
 
 def build_info():

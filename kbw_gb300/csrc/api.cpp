@@ -93,15 +93,10 @@ double host_uniform_scale(double total) {
     return scale;
 }
 
-// splitmix64 -> 52-bit uniform in [0, 1).  Used only when the caller passes
-// no draws; it is not rand's StdRng stream.
-double next_draw(Sim &s) {
-    uint64_t z = (s.rng += 0x9E3779B97F4A7C15ull);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z ^= z >> 31;
-    return (double)(z >> 12) * (1.0 / 4503599627370496.0);
-}
+// One draw of the handle's generator, used when the caller passes no draws:
+// the UniformFloat<f64> sample WeightedIndex takes from rand's StdRng
+// (src/quantum_execution.rs:279-282, src/convert.rs:60-64).
+double next_draw(Sim &s) { return s.rng.uniform01(); }
 
 template <class T>
 static cudaError_t flush_t(Sim &s) {
@@ -266,10 +261,8 @@ int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_s
     e = cudaMallocHost(&s->h_ctl, sizeof(MeasureCtl) + kMaxTerms * sizeof(double));
     if (e != cudaSuccess) return cleanup(KBWG_ENOMEM, "pinned allocation");
     s->h_result = (double *)(s->h_ctl + 1);
-    const char *seed = getenv("KBW_SEED");
-    char *end = nullptr;
-    unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
-    s->rng = (seed && end && *end == 0 && *seed) ? (uint64_t)sv : (uint64_t)(uintptr_t)s ^ 0x5DEECE66Dull;
+    // StdRng::seed_from_u64(KBW_SEED) as QubitManager::new (src/quantum_execution.rs:181-191)
+    s->rng = StdRng::seed_from_u64(kbw_seed_from_env());
     s->jit_mode = jit_default_mode();
     std::string tmsg;
     const int32_t trc = apply_env_tuning(*s, tmsg);
@@ -1045,6 +1038,19 @@ int32_t kbwg_jit_check_adjoint(uintptr_t num_qubits, int32_t precision, uint32_t
     GUARD_END
 }
 
+int32_t kbwg_chacha_block(const uint32_t *key, uint64_t counter, uint64_t stream, uint32_t rounds, uint32_t *out) {
+    if (!key || !out || rounds == 0 || (rounds & 1)) return fail(KBWG_EINVAL, "bad ChaCha arguments");
+    chacha_block(key, counter, stream, (int)rounds, out);
+    return KBWG_OK;
+}
+
+int32_t kbwg_draws(uint64_t seed, uintptr_t count, double *out) {
+    if (count && !out) return fail(KBWG_EINVAL, "null output");
+    StdRng r = StdRng::seed_from_u64(seed);
+    for (uintptr_t i = 0; i < count; i++) out[i] = r.uniform01();
+    return KBWG_OK;
+}
+
 int32_t kbwg_select_device(int32_t device) {
     CUDA_TRY(cudaSetDevice(device));
     return KBWG_OK;
@@ -1170,12 +1176,9 @@ std::vector<PoolEntry> g_pool;
 uint64_t g_pool_clock = 0;
 constexpr size_t kPoolEntries = 4;
 
-void reseed_from_env(Sim &s) {
-    const char *seed = getenv("KBW_SEED");
-    char *end = nullptr;
-    const unsigned long long sv = seed ? strtoull(seed, &end, 10) : 0;
-    if (seed && *seed && end && *end == 0) s.rng = (uint64_t)sv;
-}
+// A fresh QubitManager's generator: StdRng::seed_from_u64(KBW_SEED), or a
+// random seed when KBW_SEED is not a u64 (src/quantum_execution.rs:181-191).
+void reseed_from_env(Sim &s) { s.rng = StdRng::seed_from_u64(kbw_seed_from_env()); }
 }  // namespace
 
 // A reset register for (current device, n, precision, flags); *pooled says

@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "stdrng.h"
 
 namespace kbwg {
 
@@ -65,7 +66,7 @@ struct Sim {
     double *h_result = nullptr;   // pinned, kMaxTerms entries
     DevBuf tmp0, tmp1, tmp2, tmp3, tmp4, tmp5;
 
-    uint64_t rng = 0;  // splitmix64 state of the handle's own draw generator
+    StdRng rng;  // the handle's own draw generator (rand's StdRng, seeded from KBW_SEED)
 
     Profiler prof;
     void *graphs = nullptr;  // replay cache of planned sweeps (sweep.cu)

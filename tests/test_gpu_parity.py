@@ -534,3 +534,25 @@ def test_folded_diagonal_chains(prec, fast):
         sim.apply(circ)
         assert rel_err(sim.state(), ref.state()) < (1e-12 if prec == "c128" else 1e-5)
         sim.close()
+
+
+def test_own_generator_is_stdrng_of_kbw_seed(monkeypatch):
+    """Without caller draws a handle draws from StdRng::seed_from_u64(KBW_SEED)
+    (the reference QubitManager's generator): the outcomes equal those with
+    the same stream passed explicitly; sampling continues the stream."""
+    from kbw_gb300 import _native as N
+    monkeypatch.setenv("KBW_SEED", "20260704")
+    n = 10
+    circ = C.random_circuit(n, 120, 31, max_controls=1)
+    qs = list(range(n))
+    a = DenseGB300(n, "c128")
+    a.apply(circ)
+    own = [a.measure(qs) for _ in range(1)] + [a.sample(qs, 64)]
+    b = DenseGB300(n, "c128")
+    b.apply(circ)
+    d = N.draws(20260704, n + 64)
+    given = [b.measure(qs, d[:n])] + [b.sample(qs, 64, d[n:])]
+    assert own[0] == given[0]
+    assert np.array_equal(own[1][0], given[1][0]) and np.array_equal(own[1][1], given[1][1])
+    a.close()
+    b.close()
