@@ -456,6 +456,24 @@ def run_batch_bench(args, torch, C):
 PARITY_PARAMS = 24
 
 
+def run_wide_register(args, torch, DenseGB300, C, peak):
+    """Past Dense's 32 qubits: the brickwork on 33 qubits in complex128
+    float-float (128 GiB of amplitudes, 64-bit state indices), CUDA-event
+    time per step and per sweep against the HBM roofline."""
+    n, layers = 33, args.layers
+    circ = C.brickwork(n, layers, 0)
+    sim = DenseGB300(n, "c128", fast_c128=True)
+    ms, nl, kms, kb = time_steps(sim, circ, 2, 2, torch)
+    passes = sim.last_flush_stats()[1]
+    sim.close()
+    ach = kb / (kms * 1e-3) / 1e9
+    return {"config": "brickwork-%dq-%dlayers-c128 (float-float)" % (n, layers), "gates": len(circ),
+            "state_gib": (16 << n) >> 30, "ms_per_step": round(ms, 2), "sweeps_per_step": passes,
+            "value": round(len(circ) * 2 * 16 * (1 << n) / (ms * 1e-3) / 1e9, 1), "unit": "GB/s",
+            "roofline": {"achieved": round(ach, 1), "frac": round(ach / peak, 4),
+                         "avg_launch_ms": round(kms / max(nl, 1), 3)}}
+
+
 def parity_param_picks(n, layers, count=PARITY_PARAMS):
     """`count` parameters of the hardware-efficient ansatz spread over every
     layer, alternating RY and RZ, on varying qubits."""
@@ -778,6 +796,8 @@ def run_ours(args, world, rank, local):
         secondary["adjoint"] = run_adjoint_bench(args, torch, DenseGB300, C, adj_grads)
     if args.adjoint_large:
         secondary["adjoint_large"] = run_adjoint_large(args, torch, DenseGB300, C)
+    if args.wide and rank == 0:
+        secondary["register_33q"] = run_wide_register(args, torch, DenseGB300, C, peak)
     # (joined before the batch and Grover items, which run the oracle on the host)
     if checker is not None:
         secondary["parity_vs_oracle"] = parity_report(checker, args, torch, DenseGB300, C, circ, n, adj_grads)
@@ -820,6 +840,8 @@ def main():
                     help="complex128 gate arithmetic: float-float (default) or IEEE binary64")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-wide", dest="wide", action="store_false",
+                    help="skip the 33-qubit (128 GiB) register line")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the oracle parity checks at the benchmark sizes (30q state, 24q gradients)")
     ap.add_argument("--no-tune", dest="tune", action="store_false",

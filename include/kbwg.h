@@ -39,7 +39,7 @@ typedef struct kbwg_sim kbwg_sim;
 enum {
     KBWG_OK = 0,
     KBWG_EINVAL = 1,    /* bad argument: qubit index, null pointer, size */
-    KBWG_EQUBITS = 2,   /* num_qubits out of range: KetError::ExecutionFailed in src/dense.rs:71-73 */
+    KBWG_EQUBITS = 2,   /* num_qubits out of range (above 40): KetError::ExecutionFailed as in src/dense.rs:71-73 */
     KBWG_ENOMEM = 3,    /* device or pinned-host allocation failed */
     KBWG_ECUDA = 4,     /* a CUDA runtime call failed */
     KBWG_EWEIGHT = 5,   /* all sampling weights are zero (src/convert.rs:60 panics) */
@@ -74,8 +74,12 @@ enum {
 };
 
 /* QuantumExecution::new (src/quantum_execution.rs:53; src/dense.rs:70-89).
- * Allocates 2^num_qubits amplitudes in |0...0>.  num_qubits must be <= 32
- * (KBWG_EQUBITS otherwise, as Dense::new). */
+ * Allocates 2^num_qubits amplitudes in |0...0>.  Dense::new stops at 32
+ * qubits; DenseGPU and the Block backends have no cap (src/c_api.rs:93-109),
+ * and neither has this engine below 40 (KBWG_EQUBITS above): the device's
+ * memory decides (KBWG_ENOMEM), one GB300 holding 33 qubits in complex128 or
+ * 34 in complex64.  Above 32 qubits gates run in the default tile geometry
+ * with 64-bit state indices; the adjoint gradient stays at 32 qubits. */
 int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_sim **out);
 
 /* Drop of the backend (ket frees its QPUConfig, src/c_api.rs:124). */

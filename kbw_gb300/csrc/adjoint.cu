@@ -750,6 +750,10 @@ size_t jit_check_adjoint(const Sim &s, const std::vector<GateDesc> &fwd, const s
 int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
                          const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
                          std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
+    if (s.n > 32) {  // the reverse sweeps index with 32 bits (and need three states)
+        set_error(KBWG_EUNSUPPORTED, "adjoint: at most 32 qubits");
+        return KBWG_EUNSUPPORTED;
+    }
     if (s.n < (uint32_t)AdjCfg<float>::K || (s.prec && s.n < (uint32_t)AdjCfg<double>::K)) {
         set_error(KBWG_EUNSUPPORTED, "adjoint: needs at least 12 qubits (complex64) or 11 (complex128)");
         return KBWG_EUNSUPPORTED;

@@ -225,7 +225,7 @@ int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_s
     GUARD_BEGIN
     if (!out) return fail(KBWG_EINVAL, "null out pointer");
     *out = nullptr;
-    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32 (Dense limit)");
+    if (num_qubits > kMaxQubits) return fail(KBWG_EQUBITS, "num_qubits > 40");
     if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
     kbwg_sim *s = new kbwg_sim();
     s->n = (uint32_t)num_qubits;
@@ -937,7 +937,7 @@ int32_t kbwg_plan_tuned(uintptr_t num_qubits, int32_t precision, uint32_t flags,
     if (!n_sweeps || (n_gates && (!gates || !order || !sweep_end || !tile_mask)))
         return fail(KBWG_EINVAL, "null argument");
     if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
-    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    if (num_qubits > kMaxQubits) return fail(KBWG_EQUBITS, "num_qubits > 40");
     Sim tmp;  // the geometry rules of a handle of this size, precision and flags (no device state)
     tmp.n = (uint32_t)num_qubits;
     tmp.prec = precision;
@@ -975,7 +975,7 @@ int32_t kbwg_jit_check(uintptr_t num_qubits, int32_t precision, uint32_t flags, 
     GUARD_BEGIN
     if (!n_sweeps || !n_failed || (n_gates && !gates)) return fail(KBWG_EINVAL, "null argument");
     if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
-    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    if (num_qubits > kMaxQubits) return fail(KBWG_EQUBITS, "num_qubits > 40");
     if (!jit_available()) return fail(KBWG_EUNSUPPORTED, "NVRTC (libnvrtc.so.13) not found");
     Sim tmp;  // the rules of a handle of this size, precision and flags (no device state)
     tmp.n = (uint32_t)num_qubits;
@@ -1009,7 +1009,7 @@ int32_t kbwg_jit_check_adjoint(uintptr_t num_qubits, int32_t precision, uint32_t
     GUARD_BEGIN
     if (!n_sweeps || !n_failed || (n_gates && !gates)) return fail(KBWG_EINVAL, "null argument");
     if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
-    if (num_qubits > 32) return fail(KBWG_EQUBITS, "num_qubits > 32");
+    if (num_qubits > kMaxQubits) return fail(KBWG_EQUBITS, "num_qubits > 40");
     if (!jit_available()) return fail(KBWG_EUNSUPPORTED, "NVRTC (libnvrtc.so.13) not found");
     Sim tmp;
     tmp.n = (uint32_t)num_qubits;

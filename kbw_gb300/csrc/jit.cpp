@@ -324,12 +324,13 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
     const int last = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.back();
     s += "#include \"jit_dev.cuh\"\n"
          "using namespace kbwg;\n"
-         "namespace {\n"
-         "struct Body {\n";
+         "namespace {\n";
+    s += geo.wide ? "typedef uint64_t BaseT;\n" : "typedef uint32_t BaseT;\n";
+    s += "struct Body {\n";
     s += "  static constexpr int kFirst = " + std::to_string(first) + ", kLast = " + std::to_string(last) + ";\n";
     s += "  template <class P, int K, int R>\n"
          "  static __device__ __forceinline__ void run(typename P::Amp (&v)[1 << R], typename P::Amp *tile,\n"
-         "      uint32_t FA, uint32_t FB, uint32_t base, const TileGate *sg) {\n"
+         "      uint32_t FA, uint32_t FB, BaseT base, const TileGate *sg) {\n"
          "    const typename P::K4 kz{};\n";
     s += std::string("    uint32_t F = ") + (first == LAYOUT_A ? "FA" : "FB") + ";\n";
     s += "    (void)tile; (void)base; (void)sg; (void)kz; (void)F;\n";
@@ -346,8 +347,7 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
         const size_t g1 = sw.stage_end[st];
         for (size_t i = g0; i < g1; i++) {
             const TileGate &t = sw.gates[i];
-            // (state indices fit 32 bits in the forward sweeps: at most 32 qubits)
-            s += "    " + outer_guard(t, gate_stmt(t, "v", constants_of(t, i).c_str()), false) + "\n";
+            s += "    " + outer_guard(t, gate_stmt(t, "v", constants_of(t, i).c_str()), geo.wide) + "\n";
         }
         g0 = g1;
     }
@@ -355,8 +355,8 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d)\n"
              "kbwg_jit_sweep(%s::Mem *__restrict__ st, const __grid_constant__ SweepParams p) {\n"
-             "  jit::sweep<%s, %d, %d, Body>(st, p);\n}\n",
-             geo.threads, geo.ctas_per_sm, geo.policy, geo.policy, geo.K, geo.R);
+             "  jit::sweep<%s, %d, %d, Body, %s>(st, p);\n}\n",
+             geo.threads, geo.ctas_per_sm, geo.policy, geo.policy, geo.K, geo.R, geo.wide ? "true" : "false");
     s += buf;
     return s;
 }

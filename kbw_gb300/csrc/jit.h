@@ -17,6 +17,7 @@ namespace kbwg {
 struct JitGeometry {
     const char *policy;
     int K, R, threads, ctas_per_sm;
+    bool wide = false;  // 64-bit state indices (registers above 32 qubits)
 };
 
 // Source of the kernel that applies `sw`'s gates (entry point kbwg_jit_sweep,

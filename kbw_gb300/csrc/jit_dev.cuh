@@ -133,10 +133,11 @@ __device__ __forceinline__ void relayout(typename P::Amp (&v)[1 << R], typename 
 // with a bounded wait, registers in layout Body::kFirst, coalesced stores
 // from registers in layout Body::kLast) with the gate program replaced by
 // Body::run, the sweep's gates as straight-line code.
-template <class P, int K, int R, class Body>
+template <class P, int K, int R, class Body, bool W = false>
 __device__ __forceinline__ void sweep(typename P::Mem *__restrict__ st, const SweepParams &p) {
     using Amp = typename P::Amp;
     using Mem = typename P::Mem;
+    using B = typename pick_t<W, uint64_t, uint32_t>::type;  // state index width
     constexpr int NR = 1 << R;
     constexpr size_t kTileBytes = sizeof(Mem) << K;
     constexpr size_t kChunkTable = 256 * sizeof(uint64_t);
@@ -165,8 +166,8 @@ __device__ __forceinline__ void sweep(typename P::Mem *__restrict__ st, const Sw
     __syncthreads();
 
     auto tile_base = [&](uint32_t tau) {
-        uint32_t b = tau << l;
-        for (uint32_t j = 0; j < m; j++) b = (uint32_t)insert_zero_at(b, p.hq[j]);
+        B b = (B)tau << l;
+        for (uint32_t j = 0; j < m; j++) b = (B)insert_zero_at(b, p.hq[j]);
         return b;
     };
     auto issue_load = [&](uint32_t tau) {
@@ -188,7 +189,7 @@ __device__ __forceinline__ void sweep(typename P::Mem *__restrict__ st, const Sw
     const uint32_t Ffirst = (Body::kFirst == LAYOUT_A) ? FA : FB;
     const uint32_t Flast = (Body::kLast == LAYOUT_A) ? FA : FB;
     for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
-        const uint32_t base = tile_base(tau);
+        const B base = tile_base(tau);
         if (!tile_wait(bar, it & 1u, p.err)) return;
         Amp v[NR];
 #pragma unroll

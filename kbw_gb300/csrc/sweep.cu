@@ -60,12 +60,15 @@ struct SweepKernel {
     static_assert(K <= kLaneBits + 2 * R, "tile geometry leaves local bits no layout holds in registers");
 };
 
-template <class P, int K, int R>
+// W: 64-bit state indices (registers above 32 qubits); the 32-bit form keeps
+// registers free for the amplitudes.
+template <class P, int K, int R, bool W>
 __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P, K, R>::kCtasPerSm)
     k_sweep(typename P::Mem *__restrict__ st, const __grid_constant__ SweepParams p) {
     using Amp = typename P::Amp;
     using Mem = typename P::Mem;
     using SK = SweepKernel<P, K, R>;
+    using B = typename pick_t<W, uint64_t, uint32_t>::type;
     constexpr int NR = 1 << R;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Amp *tile = reinterpret_cast<Amp *>(smem_raw);
@@ -93,11 +96,9 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
     }
     __syncthreads();
 
-    // state indices fit 32 bits (at most 32 qubits): 32-bit tile indices keep
-    // registers free for the amplitudes
     auto tile_base = [&](uint32_t tau) {
-        uint32_t b = tau << l;
-        for (uint32_t j = 0; j < m; j++) b = insert_zero_at(b, p.hq[j]);
+        B b = (B)tau << l;
+        for (uint32_t j = 0; j < m; j++) b = (B)insert_zero_at(b, p.hq[j]);
         return b;
     };
     auto issue_load = [&](uint32_t tau) {
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
     const uint32_t FA = (uint32_t)lane | ((uint32_t)warp << (kLaneBits + R));
     const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
     for (uint32_t it = 0; tau < p.tiles; tau += gridDim.x, it++) {
-        const uint32_t base = tile_base(tau);
+        const B base = tile_base(tau);
         if (!tile_wait(bar, it & 1u, p.err)) return;
         Amp v[NR];
         int layout = p.stage_layout[0];
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(SweepKernel<P, K, R>::kThreads, SweepKernel<P,
                 for (int j = 0; j < NR; j++) v[j] = tile[F | ((uint32_t)j << R0)];
             }
             const uint32_t g1 = p.stage_end[s];
-            for (uint32_t gi = g0; gi < g1; gi++) tile_gate<P, K, R>(sg[gi], v, R0, F, base);
+            for (uint32_t gi = g0; gi < g1; gi++) tile_gate<P, K, R, B>(sg[gi], v, R0, F, base);
             g0 = g1;
         }
         // the tile buffer is free: start the next tile's load, then store this one
@@ -260,17 +261,17 @@ static cudaError_t upload_program(Sim &s, const std::vector<TileGate> &planned, 
     return copy_async(dst, prog.data(), prog.size() * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
 }
 
-template <class P, int K, int R>
+template <class P, int K, int R, bool W = false>
 static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     using SK = SweepKernel<P, K, R>;
     using Mem = typename P::Mem;
     int num_sms = 0;
     {
-        cudaError_t e = ensure_smem_limit((const void *)k_sweep<P, K, R>, SK::kSmem);
+        cudaError_t e = ensure_smem_limit((const void *)k_sweep<P, K, R, W>, SK::kSmem);
         if (e == cudaSuccess) e = current_sm_count(num_sms);
         if (e != cudaSuccess) return e;
     }
-    const void *kid = (const void *)k_sweep<P, K, R>;
+    const void *kid = (const void *)k_sweep<P, K, R, W>;
     const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
     // timed profiling marks every launch with events, which a graph replay cannot
     const bool graphs_ok = !s.prof.on && !(s.flags & KBWG_FLAG_NO_GRAPHS);
@@ -354,7 +355,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
     // graph), or on every flush in KBWG_JIT_ALWAYS mode.  A sweep whose kernel
     // could not be built runs the interpreted k_sweep.
     std::vector<const void *> jk;
-    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm, W};
     bool load_jit = s.jit_mode == KBWG_JIT_ALWAYS;
     if (auto_jit && repeat) {
         if (!job) {  // start compiling this structure's kernels in the background
@@ -416,7 +417,7 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
             cudaLaunchKernel(spec, dim3((unsigned)grid), dim3(SK::kThreads), args, SK::kSmem, s.stream);
             specialised++;
         } else {
-            k_sweep<P, K, R><<<(unsigned)grid, SK::kThreads, SK::kSmem, s.stream>>>((Mem *)s.state, p);
+            k_sweep<P, K, R, W><<<(unsigned)grid, SK::kThreads, SK::kSmem, s.stream>>>((Mem *)s.state, p);
         }
         if (!graphs) count_launch();
         e = cudaGetLastError();
@@ -472,6 +473,11 @@ static cudaError_t run_fused_p(Sim &s, const GateDesc *gates, size_t count) {
 // 11 (8) and 12 (16).  The order-preserving mode has the default only.
 std::vector<uint32_t> compiled_tiles(const Sim &s) {
     if (s.flags & KBWG_FLAG_EXACT_ORDER) return {(uint32_t)(s.prec ? TileCfg<double>::K : TileCfg<float>::K)};
+    // registers above 32 qubits: the default geometry, with 64-bit state indices
+    if (s.n > 32) {
+        if (ff_capable(s)) return {(uint32_t)TileCfgFF::K};
+        return {(uint32_t)(s.prec ? TileCfg<double>::K : TileCfg<float>::K)};
+    }
     if (ff_capable(s)) return {(uint32_t)TileCfgFF::K, 12u};
     if (s.prec) return {(uint32_t)TileCfg<double>::K, 11u};
     return {(uint32_t)TileCfg<float>::K, 12u, 11u};
@@ -528,6 +534,11 @@ uint32_t effective_tile_k(const Sim &s) {
 template <class T>
 static cudaError_t run_fused_t(Sim &s, const GateDesc *gates, size_t count) {
     constexpr int K = TileCfg<T>::K, R = TileCfg<T>::R;
+    if (s.n > 32) {  // 64-bit state indices, default geometry
+        if (s.flags & KBWG_FLAG_EXACT_ORDER) return run_fused_p<Exact<T>, K, R, true>(s, gates, count);
+        if constexpr (std::is_same<T, float>::value) return run_fused_p<FastP, K, R, true>(s, gates, count);
+        else return run_fused_p<Fast<T>, K, R, true>(s, gates, count);
+    }
     const uint32_t tk = chosen_tile(s);
     if (tk != (uint32_t)K && !(s.flags & KBWG_FLAG_EXACT_ORDER)) {
         if constexpr (std::is_same<T, float>::value) {
@@ -695,7 +706,7 @@ static size_t check_p(const Sim &s, const GateDesc *gates, size_t count, size_t 
     const size_t depth = s.fusion_depth ? s.fusion_depth : (size_t)kMaxSweepGates;
     const std::vector<PlannedSweep> plan =
         plan_sweeps(s.n, K, R, gates, count, (s.flags & KBWG_FLAG_EXACT_ORDER) != 0, depth);
-    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm};
+    const JitGeometry geo{PolicyName<P>::s, K, R, SK::kThreads, SK::kCtasPerSm, s.n > 32};
     std::vector<std::string> srcs;
     for (const PlannedSweep &sw : plan) srcs.push_back(jit_sweep_source(geo, sw));
     sweeps = plan.size();
@@ -752,6 +763,7 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count) {
             s.ff_resident = true;
         }
         std::vector<GateDesc> g = ff_rewrite(gates, count);
+        if (s.n > 32) return run_fused_p<FF2, TileCfgFF::K, TileCfgFF::R, true>(s, g.data(), g.size());
         if (chosen_tile(s) == 12) return run_fused_p<FF2, 12, 4>(s, g.data(), g.size());
         return run_fused_p<FF2, TileCfgFF::K, TileCfgFF::R>(s, g.data(), g.size());
     }

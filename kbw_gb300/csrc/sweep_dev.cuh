@@ -603,15 +603,20 @@ __device__ __forceinline__ void diag_fixed(typename P::Amp (&v)[1 << R], const T
 // Apply one gate to the thread's registers.  F = the thread's fixed local
 // bits (lane and warp) in this stage's layout; base = the tile's global
 // index of local 0.  A few header loads and one jump table per gate.
-template <class P, int K, int R>
+template <class T> struct ident { using type = T; };
+template <bool W, class A, class C> struct pick_t { using type = A; };
+template <class A, class C> struct pick_t<false, A, C> { using type = C; };
+
+// B: type of the state index (32 bits up to 32 qubits, 64 bits above; not
+// deduced from the argument, so a caller names 64 bits explicitly).
+template <class P, int K, int R, class B = uint32_t>
 __device__ __forceinline__ void tile_gate(const TileGate &g, typename P::Amp (&v)[1 << R], int /*R0*/, uint32_t F,
-                                          uint32_t base) {
+                                          typename ident<B>::type base) {
     static_assert(R >= 3 && R <= 4, "dispatch covers register bits 0..3");
     const uint32_t op = g.op;
     const uint32_t fneed = g.fneed;
     const uint32_t jm = g.jm;
-    // (state indices and control masks fit 32 bits: at most 32 qubits)
-    const uint32_t co = (uint32_t)g.co;
+    const B co = (B)g.co;
     if ((base & co) != co) return;  // a control outside the tile is 0 for the whole tile
     const bool fok = (F & fneed) == fneed;
     if (op < OP_REG) {  // lane targets: every lane shuffles, outside the jump table

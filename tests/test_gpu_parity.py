@@ -556,3 +556,35 @@ def test_own_generator_is_stdrng_of_kbw_seed(monkeypatch):
     assert np.array_equal(own[1][0], given[1][0]) and np.array_equal(own[1][1], given[1][1])
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("n,prec,fast", [(33, "c128", True), (33, "c128", False), (34, "c64", False)])
+def test_registers_above_32_qubits(n, prec, fast):
+    """Beyond Dense's 32 qubits (DenseGPU and the Block backends have no cap):
+    128 GiB of amplitudes on one GB300, swept with 64-bit state indices.  A
+    random circuit with controls on the top qubits keeps the norm, its
+    inverse returns |0...0>, and a Bell pair between the top and the bottom
+    qubit reads out exactly (dump, p1, measurement with injected draws)."""
+    import gc
+    gc.collect()  # earlier tests' handles (up to 64 GiB) must be gone
+    circ = C.random_circuit(n, 90, 91, max_controls=2)
+    circ += [(C.H, n - 1, (), 0.0), (C.RY, n - 2, (n - 1,), 0.7), (C.X, 0, (n - 1, n - 2), 0.0)]
+    inv = [(k, t, c, -a if k in C.PARAMETRIC else a) for (k, t, c, a) in reversed(circ)]
+    sim = DenseGB300(n, prec, fast_c128=fast)
+    tol = 1e-12 if prec == "c128" else 2e-5
+    sim.apply(circ)
+    assert abs(sim.exp_value([(1.0, [])]) - 1.0) < tol
+    sim.apply(inv)
+    top = n - 1
+    assert sim.measure_p1(top) < tol and sim.measure_p1(n - 2) < tol and sim.measure_p1(0) < tol
+    sim.clear()
+    sim.hadamard(top)
+    sim.pauli_x(0, [top])
+    st, re, im = sim.dump([top, 0])
+    assert st.tolist() == [0, 3]
+    assert np.allclose(re, [2 ** -0.5] * 2, atol=tol) and np.allclose(im, 0.0, atol=tol)
+    assert abs(sim.measure_p1(top) - 0.5) < tol
+    assert sim.measure([top, 0], [0.75, 0.1]) in (0, 3)
+    sim.close()
+    del sim
+    gc.collect()
