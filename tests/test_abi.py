@@ -47,7 +47,7 @@ def test_new_without_gpu_fails_cleanly(lib, cuda_available):
     h = ctypes.c_void_p()
     code = lib.kbwg_new(4, N.C64, 0, ctypes.byref(h))
     assert code != N.OK and not h.value
-    assert lib.kbwg_new(33, N.C64, 0, ctypes.byref(h)) == N.EQUBITS
+    assert lib.kbwg_new(41, N.C64, 0, ctypes.byref(h)) == N.EQUBITS
 
 
 def replay(n, circuit, prec):
