@@ -39,7 +39,7 @@ static int no_gpu(void) {
     OK(kbwg_build_info(&msg, &len));
     CHECK(len > 0 && memcmp(msg, "kbw-gb300", 9) == 0, "build info");
     kbwg_sim *sim = (kbwg_sim *)0x1;
-    CHECK(kbwg_new(33, KBWG_C64, 0, &sim) == KBWG_EQUBITS && sim == NULL, "33 qubits must be EQUBITS");
+    CHECK(kbwg_new(41, KBWG_C64, 0, &sim) == KBWG_EQUBITS && sim == NULL, "41 qubits must be EQUBITS");
     sim = (kbwg_sim *)0x1;
     int32_t rc = kbwg_new(4, KBWG_C128, 0, &sim);
     CHECK(rc != KBWG_OK && sim == NULL, "kbwg_new without a GPU must fail cleanly (rc %d)", (int)rc);

@@ -266,8 +266,11 @@ def test_clear_and_state_roundtrip():
 
 def test_errors_are_status_codes():
     with pytest.raises(KbwgError) as e:
-        DenseGB300(33, "c64")
+        DenseGB300(41, "c64")
     assert e.value.code == 2
+    with pytest.raises(KbwgError) as e:  # 16 TiB: the device's memory refuses it
+        DenseGB300(40, "c128")
+    assert e.value.code == 3
     sim = DenseGB300(4, "c64")
     with pytest.raises(KbwgError):
         sim.pauli_x(4)
