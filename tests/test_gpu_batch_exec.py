@@ -88,7 +88,7 @@ def test_batch_gradient_equals_handle_adjoint(prec, fast):
 def test_batch_errors_and_release():
     circ = C.random_circuit(12, 50, 1)
     with pytest.raises(KbwgError) as ei:
-        batch_exp_value(33, [], [C.tfim_ring(4)])
+        batch_exp_value(41, [], [C.tfim_ring(4)])
     assert ei.value.code == N.EQUBITS
     with pytest.raises(KbwgError) as ei:
         batch_sample(12, circ, [], 10, C.uniform_draws(10, 1))
