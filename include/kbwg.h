@@ -249,6 +249,26 @@ int32_t kbwg_batch_gradient(uintptr_t num_qubits, int32_t precision, uint32_t fl
 /* Free the pooled registers no call is using. */
 int32_t kbwg_batch_release(void);
 
+/* Many BatchExecution::exp_value requests (src/quantum_execution.rs:392-405,
+ * each of which the reference runs on a fresh simulator) in one persistent
+ * launch: circuit c has num_qubits[c] qubits (1..24), the gates
+ * gates[gate_offsets[c] .. gate_offsets[c+1]) (as for kbwg_apply_gates) and
+ * the Hamiltonian made of the strings [ham_offsets[c], ham_offsets[c+1]) of
+ * the flattened string arrays (string k: paulis/qubits
+ * [term_offsets[k], term_offsets[k+1]) with coefficient coefficients[k], as
+ * for kbwg_exp_value); energies[c] = <H_c> after the circuit from |0...0>.
+ * gate_offsets and ham_offsets have n_circuits + 1 entries.  precision:
+ * KBWG_C64, or KBWG_C128 (flags: KBWG_FLAG_FAST_C128 for float-float gate
+ * arithmetic).  Every circuit is planned into tile sweeps on the host;
+ * persistent CTAs take the circuits largest first, a register of at most 12
+ * (complex64) / 11 (complex128) qubits held on the SM, larger ones in a
+ * per-CTA global slot.  <H> accumulates FP64-grade. */
+int32_t kbwg_batch_circuits_exp_value(uintptr_t n_circuits, int32_t precision, uint32_t flags,
+                                      const uint32_t *num_qubits, const kbwg_gate *gates,
+                                      const uintptr_t *gate_offsets, const uint8_t *paulis, const uintptr_t *qubits,
+                                      const uintptr_t *term_offsets, const double *coefficients,
+                                      const uintptr_t *ham_offsets, double *energies);
+
 /* QuantumExecution::clear (src/quantum_execution.rs:161; src/dense.rs:399-406). */
 int32_t kbwg_clear(kbwg_sim *sim);
 

@@ -106,6 +106,9 @@ SIGNATURES = {
     "kbwg_batch_gradient": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(Gate), _U, ctypes.POINTER(ctypes.c_int32),
                                    _U, ctypes.POINTER(ctypes.c_uint8), _UP, _UP, _DP, _U, ctypes.c_uint32, _DP, _DP]),
     "kbwg_batch_release": (_I32, []),
+    "kbwg_batch_circuits_exp_value": (_I32, [_U, _I32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
+                                             ctypes.POINTER(Gate), _UP, ctypes.POINTER(ctypes.c_uint8), _UP, _UP,
+                                             _DP, _UP, _DP]),
     "kbwg_tile_options": (_I32, [_P, ctypes.POINTER(ctypes.c_uint32), _U, _UP]),
     "kbwg_set_tuning": (_I32, [_P, ctypes.c_uint32, ctypes.c_uint32]),
     "kbwg_get_tuning": (_I32, [_P, ctypes.c_void_p]),

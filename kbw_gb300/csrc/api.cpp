@@ -1306,6 +1306,25 @@ int32_t kbwg_batch_gradient(uintptr_t num_qubits, int32_t precision, uint32_t fl
     GUARD_END
 }
 
+int32_t kbwg_batch_circuits_exp_value(uintptr_t n_circuits, int32_t precision, uint32_t flags,
+                                      const uint32_t *num_qubits, const kbwg_gate *gates,
+                                      const uintptr_t *gate_offsets, const uint8_t *paulis, const uintptr_t *qubits,
+                                      const uintptr_t *term_offsets, const double *coefficients,
+                                      const uintptr_t *ham_offsets, double *energies) {
+    GUARD_BEGIN
+    if (n_circuits == 0) return KBWG_OK;
+    if (!num_qubits || !gate_offsets || !ham_offsets || !energies) return fail(KBWG_EINVAL, "null argument");
+    if (precision != KBWG_C64 && precision != KBWG_C128) return fail(KBWG_EINVAL, "bad precision");
+    if (gate_offsets[n_circuits] > gate_offsets[0] && !gates) return fail(KBWG_EINVAL, "null gate list");
+    const uintptr_t nstr = ham_offsets[n_circuits];
+    if (nstr > ham_offsets[0] && (!term_offsets || !coefficients)) return fail(KBWG_EINVAL, "null Hamiltonian arrays");
+    if (nstr > ham_offsets[0] && term_offsets[nstr] > term_offsets[0] && (!paulis || !qubits))
+        return fail(KBWG_EINVAL, "null Pauli arrays");
+    return batch_circuits(precision, flags, n_circuits, num_qubits, gates, gate_offsets, paulis, qubits,
+                          term_offsets, coefficients, ham_offsets, energies);
+    GUARD_END
+}
+
 int32_t kbwg_batch_release(void) {
     GUARD_BEGIN
     std::vector<kbwg_sim *> idle;

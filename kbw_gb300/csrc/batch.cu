@@ -1,0 +1,452 @@
+// Many independent circuits in one persistent launch, each with its own
+// gate list and Pauli-string Hamiltonian: the <H> of every circuit.
+//
+// The reference answers each request of BatchExecution::exp_value with a
+// fresh simulator that replays the gates and sums the strings
+// (kbw src/quantum_execution.rs:392-405, 109-158).  Here the host plans
+// every circuit with the sweep planner (planner.cpp) into the gate programs
+// the tile kernels run, and persistent CTAs take circuits from a queue
+// sorted by cost (largest first):
+//   * n <= K: the circuit runs on a K-qubit tile that never leaves the SM
+//     (qubits n..K-1 stay |0>), its sweeps applied to the tile in registers
+//     and shared memory;
+//   * n > K: the state lives in the CTA's slot of a global buffer; every
+//     planned sweep walks the slot tile by tile (TMA bulk loads, bounded
+//     waits, coalesced stores), as k_sweep walks a handle's state.
+// <H> = sum_k c_k <P_k> with P = i^{ny} X^x Z^z: the strings are grouped by
+// flip mask x, and for each group one loop over the amplitudes forms
+// conj(a_s) a_{s^x} once and adds every string's signed share, accumulated
+// FP64-grade.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/kbwg.h"
+#include "kernels.h"
+#include "sim.h"
+#include "sweep_dev.cuh"
+
+namespace kbwg {
+
+struct BatchSweep {
+    uint32_t l, m, nstages, gate_count;
+    uint32_t gate_off, pad;
+    uint8_t hq[16];
+    uint8_t stage_layout[kMaxStages];
+    uint16_t stage_end[kMaxStages];
+};
+
+struct BatchJob {
+    uint32_t n, nsweeps, sweep_off, nterms;
+    uint32_t term_off, id;
+};
+
+struct BatchTerm {
+    uint64_t x, z;
+    double cr, ci;  // c_k * i^{ny}: the string's share of conj(a_s) a_{s^x} is sign * (cr p.re - ci p.im)
+};
+
+struct BatchArgs {
+    const BatchJob *jobs;
+    uint32_t njobs;
+    unsigned *next;
+    const BatchSweep *sweeps;
+    const TileGate *prog;
+    const BatchTerm *terms;
+    double *energies;
+    void *slots;
+    uint64_t slot_elems;
+    int *err;
+};
+
+template <class P, int K, int R>
+struct BatchKernel {
+    using Mem = typename P::Mem;
+    static constexpr int kThreads = 32 << (K - kLaneBits - R);
+    static constexpr size_t kTileBytes = sizeof(Mem) << K;
+    static constexpr size_t kSmem = kTileBytes + 256 * sizeof(uint64_t) + kMaxSweepGates * sizeof(TileGate) + 64 +
+                                    32 * 8 + 64;
+};
+
+// FP64-grade sum of float shares (short float runs, then widened) or of
+// double shares
+template <class T> struct BatchAcc {
+    double v = 0.0;
+    T part = (T)0;
+    int cnt = 0;
+    __device__ __forceinline__ void add(T x) {
+        part += x;
+        if (++cnt == 16) {
+            v += (double)part;
+            part = (T)0;
+            cnt = 0;
+        }
+    }
+    __device__ __forceinline__ double value() { return v + (double)part; }
+};
+
+template <class Mem>
+__device__ __forceinline__ Mem batch_basis(bool one) {
+    Mem m;
+    m.re = one ? 1 : 0;
+    m.im = 0;
+    return m;
+}
+
+template <class P, int K, int R>
+__global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_circuits(const __grid_constant__ BatchArgs a) {
+    using Amp = typename P::Amp;
+    using Mem = typename P::Mem;
+    using T = decltype(Mem{}.re);
+    using BK = BatchKernel<P, K, R>;
+    constexpr int NR = 1 << R;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Amp *tile = reinterpret_cast<Amp *>(smem_raw);
+    Mem *tile_mem = reinterpret_cast<Mem *>(smem_raw);
+    unsigned char *q = smem_raw + BK::kTileBytes;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(q);
+    q += 256 * sizeof(uint64_t);
+    TileGate *sg = reinterpret_cast<TileGate *>(q);
+    q += kMaxSweepGates * sizeof(TileGate);
+    uint32_t *meta = reinterpret_cast<uint32_t *>(q);
+    q += 64;
+    double *red = reinterpret_cast<double *>(q);
+    q += 32 * 8;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(q);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t FA = (uint32_t)lane | ((uint32_t)warp << (kLaneBits + R));
+    const uint32_t FB = (uint32_t)lane | ((uint32_t)warp << kLaneBits);
+    Mem *slot = reinterpret_cast<Mem *>(a.slots) + (size_t)blockIdx.x * a.slot_elems;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    uint32_t phase = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) meta[0] = atomicAdd(a.next, 1u);
+        __syncthreads();
+        const uint32_t jix = meta[0];
+        if (jix >= a.njobs) break;
+        const BatchJob job = a.jobs[jix];
+        const uint32_t n = job.n;
+        const bool in_tile = n <= (uint32_t)K;
+        // ---- |0...0> ----
+        if (in_tile) {
+            for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x) tile[u] = P::from_mem(batch_basis<Mem>(u == 0));
+        } else {
+            for (uint64_t s = threadIdx.x; s < (1ull << n); s += blockDim.x) slot[s] = batch_basis<Mem>(s == 0);
+            asm volatile("fence.proxy.async;" ::: "memory");  // generic stores before the sweeps' TMA reads
+        }
+        __syncthreads();
+        // ---- the planned sweeps ----
+        for (uint32_t sw = 0; sw < job.nsweeps; sw++) {
+            const BatchSweep &bs = a.sweeps[job.sweep_off + sw];
+            const uint32_t l = bs.l, m = bs.m, nst = bs.nstages;
+            for (uint32_t i = threadIdx.x; i < bs.gate_count; i += blockDim.x) sg[i] = a.prog[bs.gate_off + i];
+            for (uint32_t c = threadIdx.x; c < (1u << m); c += blockDim.x) {
+                uint64_t off = 0;
+                for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << bs.hq[j];
+                chunk_off[c] = off;
+            }
+            __syncthreads();
+            const uint64_t tiles = in_tile ? 1ull : (1ull << (n - K));
+            const uint32_t chunk = 1u << l, nchunks = 1u << m;
+            const uint64_t lowmask = chunk - 1;
+            for (uint64_t tau = 0; tau < tiles; tau++) {
+                uint64_t base = tau << l;
+                for (uint32_t j = 0; j < m; j++) base = insert_zero_at(base, bs.hq[j]);
+                int layout = bs.stage_layout[0];
+                int R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
+                uint32_t F = (layout == LAYOUT_A) ? FA : FB;
+                Amp v[NR];
+                if (in_tile) {
+#pragma unroll
+                    for (int j = 0; j < NR; j++) v[j] = tile[F | ((uint32_t)j << R0)];
+                } else {
+                    if (warp == 0) {
+                        if (lane == 0) mbar_expect_tx(bar, (uint32_t)BK::kTileBytes);
+                        __syncwarp();
+                        for (uint32_t c = lane; c < nchunks; c += 32)
+                            tma_load(tile_mem + (size_t)c * chunk, slot + base + chunk_off[c],
+                                     chunk * (uint32_t)sizeof(Mem), bar);
+                    }
+                    if (!tile_wait(bar, phase & 1u, a.err)) return;
+                    phase++;
+#pragma unroll
+                    for (int j = 0; j < NR; j++) v[j] = P::from_mem(tile_mem[F | ((uint32_t)j << R0)]);
+                }
+                uint32_t g0 = 0;
+                for (uint32_t s = 0; s < nst; s++) {
+                    const int nl = bs.stage_layout[s];
+                    if (nl != layout) {
+#pragma unroll
+                        for (int j = 0; j < NR; j++) tile[F | ((uint32_t)j << R0)] = v[j];
+                        __syncthreads();
+                        layout = nl;
+                        R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
+                        F = (layout == LAYOUT_A) ? FA : FB;
+#pragma unroll
+                        for (int j = 0; j < NR; j++) v[j] = tile[F | ((uint32_t)j << R0)];
+                    }
+                    const uint32_t g1 = bs.stage_end[s];
+                    for (uint32_t gi = g0; gi < g1; gi++) tile_gate<P, K, R, uint64_t>(sg[gi], v, R0, F, base);
+                    g0 = g1;
+                }
+                if (in_tile) {
+                    // every thread rewrites the positions it read in this layout
+#pragma unroll
+                    for (int j = 0; j < NR; j++) tile[F | ((uint32_t)j << R0)] = v[j];
+                } else {
+                    // the tile buffer is read no more (next tile's load) once all threads pass here
+                    fence_proxy_async();
+                    __syncthreads();
+#pragma unroll
+                    for (int j = 0; j < NR; j++) {
+                        const uint32_t u = F | ((uint32_t)j << R0);
+                        slot[base + chunk_off[u >> l] + (u & lowmask)] = P::to_mem(v[j]);
+                    }
+                }
+            }
+            if (!in_tile) asm volatile("fence.proxy.async;" ::: "memory");  // this sweep's stores before the next's loads
+            __syncthreads();
+        }
+        // ---- <H> ----
+        BatchAcc<T> acc;
+        const uint64_t ns = 1ull << n;
+        for (uint32_t t0 = 0; t0 < job.nterms;) {
+            const uint64_t x = a.terms[job.term_off + t0].x;
+            uint32_t t1 = t0 + 1;
+            while (t1 < job.nterms && a.terms[job.term_off + t1].x == x) t1++;
+            for (uint64_t s = threadIdx.x; s < ns; s += blockDim.x) {
+                Mem as, ax;
+                if (in_tile) {
+                    as = P::to_mem(tile[s]);
+                    ax = P::to_mem(tile[s ^ x]);
+                } else {
+                    as = slot[s];
+                    ax = slot[s ^ x];
+                }
+                // conj(a_s) a_{s^x}
+                const T pr = as.re * ax.re + as.im * ax.im, pi = as.re * ax.im - as.im * ax.re;
+                T share = (T)0;
+                for (uint32_t k = t0; k < t1; k++) {
+                    const BatchTerm &tk = a.terms[job.term_off + k];
+                    const T w = (T)tk.cr * pr - (T)tk.ci * pi;
+                    share += (__popcll((s ^ x) & tk.z) & 1) ? -w : w;
+                }
+                acc.add(share);
+            }
+            t0 = t1;
+        }
+        double e = acc.value();
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+        if (lane == 0) red[warp] = e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w2 = 0; w2 < (int)(blockDim.x >> 5); w2++) t += red[w2];
+            a.energies[job.id] = t;
+        }
+    }
+}
+
+// ---- host side -----------------------------------------------------------------------
+struct BatchCircuitIn {
+    uint32_t n;
+    std::vector<GateDesc> gates;
+    std::vector<BatchTerm> terms;
+};
+
+template <class P, int K, int R>
+static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, double *energies) {
+    using BK = BatchKernel<P, K, R>;
+    using Mem = typename P::Mem;
+    auto fail = [](cudaError_t e, const char *what) {
+        cudaGetLastError();
+        set_error(e == cudaErrorMemoryAllocation ? KBWG_ENOMEM : KBWG_ECUDA,
+                  std::string("batch circuits: ") + what + ": " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? (int32_t)KBWG_ENOMEM : (int32_t)KBWG_ECUDA;
+    };
+    (void)prec;
+    std::vector<BatchJob> jobs;
+    std::vector<BatchSweep> sweeps;
+    std::vector<TileGate> prog;
+    std::vector<BatchTerm> terms;
+    uint32_t nmax = 0;
+    for (size_t c = 0; c < circs.size(); c++) {
+        const BatchCircuitIn &ci = circs[c];
+        const uint32_t nplan = std::max<uint32_t>(ci.n, (uint32_t)K);  // small registers padded with |0> qubits
+        const std::vector<PlannedSweep> plan =
+            plan_sweeps(nplan, K, R, ci.gates.data(), ci.gates.size(), false, kMaxSweepGates);
+        size_t placed = 0;
+        BatchJob j;
+        memset(&j, 0, sizeof j);
+        j.n = ci.n;
+        j.id = (uint32_t)c;
+        j.sweep_off = (uint32_t)sweeps.size();
+        j.nsweeps = (uint32_t)plan.size();
+        for (const PlannedSweep &sw : plan) {
+            BatchSweep b;
+            memset(&b, 0, sizeof b);
+            b.l = sw.l;
+            b.m = sw.m;
+            memcpy(b.hq, sw.hq, sizeof b.hq);
+            b.nstages = (uint32_t)sw.stage_layout.size();
+            b.gate_count = (uint32_t)sw.gates.size();
+            b.gate_off = (uint32_t)prog.size();
+            for (uint32_t i = 0; i < b.nstages; i++) {
+                b.stage_layout[i] = sw.stage_layout[i];
+                b.stage_end[i] = sw.stage_end[i];
+            }
+            for (TileGate t : sw.gates) {
+                P::pack_host(t);
+                prog.push_back(t);
+            }
+            placed += sw.gates.size();
+            sweeps.push_back(b);
+        }
+        if (placed != ci.gates.size()) {
+            set_error(KBWG_EINVAL, "batch circuits: the planner could not place a circuit's gates");
+            return KBWG_EINVAL;
+        }
+        j.term_off = (uint32_t)terms.size();
+        j.nterms = (uint32_t)ci.terms.size();
+        std::vector<BatchTerm> t = ci.terms;
+        std::stable_sort(t.begin(), t.end(), [](const BatchTerm &x, const BatchTerm &y) { return x.x < y.x; });
+        terms.insert(terms.end(), t.begin(), t.end());
+        jobs.push_back(j);
+        nmax = std::max(nmax, ci.n);
+    }
+    // largest first: the persistent CTAs then finish together
+    std::stable_sort(jobs.begin(), jobs.end(), [&](const BatchJob &x, const BatchJob &y) {
+        const double cx = (double)(1ull << x.n) * (1.0 + x.nsweeps + 0.25 * x.nterms);
+        const double cy = (double)(1ull << y.n) * (1.0 + y.nsweeps + 0.25 * y.nterms);
+        return cx > cy;
+    });
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = ensure_smem_limit((const void *)k_batch_circuits<P, K, R>, BK::kSmem);
+    if (e != cudaSuccess) return fail(e, "setup");
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_circuits<P, K, R>, BK::kThreads, BK::kSmem);
+    if (e != cudaSuccess) return fail(e, "occupancy");
+    const uint32_t grid = (uint32_t)std::min<size_t>(jobs.size(), (size_t)sms * std::max(occ, 1));
+    const uint64_t slot_elems = nmax > (uint32_t)K ? (1ull << nmax) : 0;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t jb = jobs.size() * sizeof(BatchJob), swb = std::max<size_t>(sweeps.size(), 1) * sizeof(BatchSweep),
+                 pb = std::max<size_t>(prog.size(), 1) * sizeof(TileGate),
+                 tb = std::max<size_t>(terms.size(), 1) * sizeof(BatchTerm), eb = circs.size() * sizeof(double),
+                 sb = (size_t)grid * slot_elems * sizeof(Mem);
+    const size_t o_sw = up(jb), o_p = o_sw + up(swb), o_t = o_p + up(pb), o_e = o_t + up(tb), o_c = o_e + up(eb),
+                 o_err = o_c + 256, o_s = o_err + 256;
+    cudaStream_t st = nullptr;
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(e, "stream");
+    char *dbuf = nullptr;
+    e = cudaMalloc(&dbuf, o_s + sb);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(st);
+        return fail(e, "buffers");
+    }
+    BatchArgs a;
+    memset(&a, 0, sizeof a);
+    a.jobs = (const BatchJob *)dbuf;
+    a.njobs = (uint32_t)jobs.size();
+    a.next = (unsigned *)(dbuf + o_c);
+    a.sweeps = (const BatchSweep *)(dbuf + o_sw);
+    a.prog = (const TileGate *)(dbuf + o_p);
+    a.terms = (const BatchTerm *)(dbuf + o_t);
+    a.energies = (double *)(dbuf + o_e);
+    a.slots = dbuf + o_s;
+    a.slot_elems = slot_elems;
+    a.err = (int *)(dbuf + o_err);
+    int err_flag = 0;
+    e = copy_async(dbuf, jobs.data(), jb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !sweeps.empty())
+        e = copy_async(dbuf + o_sw, sweeps.data(), sweeps.size() * sizeof(BatchSweep), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !prog.empty())
+        e = copy_async(dbuf + o_p, prog.data(), prog.size() * sizeof(TileGate), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !terms.empty())
+        e = copy_async(dbuf + o_t, terms.data(), terms.size() * sizeof(BatchTerm), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dbuf + o_c, 0, 512, st);
+    if (e == cudaSuccess) {
+        k_batch_circuits<P, K, R><<<grid, BK::kThreads, BK::kSmem, st>>>(a);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = copy_async(energies, a.energies, eb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = copy_async(&err_flag, a.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dbuf);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(e, "run");
+    if (err_flag) {
+        set_error(KBWG_ETIMEOUT, "batch circuits: a bounded device-side wait ran out");
+        return KBWG_ETIMEOUT;
+    }
+    return KBWG_OK;
+}
+
+constexpr uint32_t kBatchMaxQubits = 24;
+
+int32_t batch_circuits(int precision, uint32_t flags, size_t ncirc, const uint32_t *num_qubits, const kbwg_gate *gates,
+                       const uintptr_t *gate_offsets, const uint8_t *paulis, const uintptr_t *qubits,
+                       const uintptr_t *term_offsets, const double *coefficients, const uintptr_t *ham_offsets,
+                       double *energies) {
+    std::vector<BatchCircuitIn> circs(ncirc);
+    for (size_t c = 0; c < ncirc; c++) {
+        BatchCircuitIn &ci = circs[c];
+        const uint32_t n = num_qubits[c];
+        if (n < 1 || n > kBatchMaxQubits) {
+            set_error(KBWG_EQUBITS, "batch circuits: every circuit needs 1..24 qubits");
+            return KBWG_EQUBITS;
+        }
+        ci.n = n;
+        if (gate_offsets[c + 1] < gate_offsets[c] || ham_offsets[c + 1] < ham_offsets[c]) {
+            set_error(KBWG_EINVAL, "batch circuits: offsets must not decrease");
+            return KBWG_EINVAL;
+        }
+        for (uintptr_t i = gate_offsets[c]; i < gate_offsets[c + 1]; i++) {
+            const kbwg_gate &g = gates[i];
+            if (g.kind > KBWG_RZ || g.target >= n || (g.control_mask >> n) || (g.control_mask & (1ull << g.target))) {
+                set_error(KBWG_EINVAL, "batch circuits: bad gate (kind, target or controls)");
+                return KBWG_EINVAL;
+            }
+            ci.gates.push_back(make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle));
+        }
+        for (uintptr_t k = ham_offsets[c]; k < ham_offsets[c + 1]; k++) {
+            BatchTerm t;
+            memset(&t, 0, sizeof t);
+            int ny = 0;
+            for (uintptr_t i = term_offsets[k]; i < term_offsets[k + 1]; i++) {
+                if (qubits[i] >= n || paulis[i] < 1 || paulis[i] > 3) {
+                    set_error(KBWG_EINVAL, "batch circuits: bad Pauli code or qubit");
+                    return KBWG_EINVAL;
+                }
+                const uint64_t b = 1ull << qubits[i];
+                if ((t.x | t.z) & b) {
+                    set_error(KBWG_EINVAL, "batch circuits: a string names a qubit twice");
+                    return KBWG_EINVAL;
+                }
+                if (paulis[i] == 1) t.x |= b;
+                else if (paulis[i] == 2) t.x |= b, t.z |= b, ny++;
+                else t.z |= b;
+            }
+            static const double re[4] = {1, 0, -1, 0}, im[4] = {0, 1, 0, -1};
+            t.cr = coefficients[k] * re[ny & 3];
+            t.ci = coefficients[k] * im[ny & 3];
+            ci.terms.push_back(t);
+        }
+    }
+    if (ncirc == 0) return KBWG_OK;
+    if (precision == KBWG_C64) return batch_run<FastP, 12, 4>(precision, circs, energies);
+    if (flags & KBWG_FLAG_FAST_C128) return batch_run<FF2B, 11, 3>(precision, circs, energies);
+    return batch_run<Fast<double>, 11, 3>(precision, circs, energies);
+}
+
+}  // namespace kbwg

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/kbwg.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "stdrng.h"
@@ -161,6 +162,12 @@ struct PauliString {
 int32_t hea_batch(int precision, bool fast_c128, size_t ncirc, const uint32_t *num_qubits, const uint32_t *layers,
                   const uint64_t *param_offset, const double *params, size_t nparams, double zz, double xc,
                   double *energies);
+
+// Many circuits with their own gates and Pauli Hamiltonians in one launch (batch.cu).
+int32_t batch_circuits(int precision, uint32_t flags, size_t ncirc, const uint32_t *num_qubits,
+                       const kbwg_gate *gates, const uintptr_t *gate_offsets, const uint8_t *paulis,
+                       const uintptr_t *qubits, const uintptr_t *term_offsets, const double *coefficients,
+                       const uintptr_t *ham_offsets, double *energies);
 
 // Adjoint gradient (adjoint.cu).  fwd: the circuit; angles: each gate's
 // angle; gtype: GT_* per gate (GT_NONE if not differentiated).  Writes E and

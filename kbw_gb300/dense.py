@@ -391,6 +391,36 @@ def batch_gradient(num_qubits, circuit, param_index, n_params, hamiltonian, prec
     return e.value, g[: int(n_params)]
 
 
+def batch_circuits_exp_value(circuits, prec="c64", fast_c128=False):
+    """<H> of many circuits in one launch: circuits is a list of
+    (num_qubits, gate list, hamiltonian); returns one energy per circuit."""
+    nq = np.ascontiguousarray([int(c[0]) for c in circuits], dtype=np.uint32)
+    gates = [g for c in circuits for g in c[1]]
+    goff = np.zeros(len(circuits) + 1, np.uintp)
+    goff[1:] = np.cumsum([len(c[1]) for c in circuits])
+    paulis, qubits, toff, coefs, hoff = [], [], [0], [], [0]
+    for c in circuits:
+        for coef, terms in c[2]:
+            for p, q in terms:
+                paulis.append(p)
+                qubits.append(q)
+            toff.append(len(paulis))
+            coefs.append(coef)
+        hoff.append(len(coefs))
+    ga = _gate_array(gates) if gates else None
+    pa = np.ascontiguousarray(paulis if paulis else [0], dtype=np.uint8)
+    qa = np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp)
+    ta = np.ascontiguousarray(toff, dtype=np.uintp)
+    ca = np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64)
+    ha = np.ascontiguousarray(hoff, dtype=np.uintp)
+    e = np.zeros(max(len(circuits), 1), np.float64)
+    N.check(N.load().kbwg_batch_circuits_exp_value(
+        len(circuits), _DT[prec][0], N.FLAG_FAST_C128 if fast_c128 else 0, _p(nq, ctypes.c_uint32), ga,
+        _p(goff, ctypes.c_size_t), _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t), _p(ta, ctypes.c_size_t),
+        _p(ca, ctypes.c_double), _p(ha, ctypes.c_size_t), _p(e, ctypes.c_double)))
+    return e[: len(circuits)]
+
+
 def batch_release():
     """Free the registers the batch entries keep between calls."""
     N.check(N.load().kbwg_batch_release())
