@@ -391,9 +391,9 @@ def batch_gradient(num_qubits, circuit, param_index, n_params, hamiltonian, prec
     return e.value, g[: int(n_params)]
 
 
-def batch_circuits_exp_value(circuits, prec="c64", fast_c128=False):
-    """<H> of many circuits in one launch: circuits is a list of
-    (num_qubits, gate list, hamiltonian); returns one energy per circuit."""
+def batch_circuits_prepare(circuits):
+    """The C arrays of kbwg_batch_circuits_exp_value for a list of
+    (num_qubits, gate list, hamiltonian) (done once; see batch_circuits_run)."""
     nq = np.ascontiguousarray([int(c[0]) for c in circuits], dtype=np.uint32)
     gates = [g for c in circuits for g in c[1]]
     goff = np.zeros(len(circuits) + 1, np.uintp)
@@ -407,18 +407,29 @@ def batch_circuits_exp_value(circuits, prec="c64", fast_c128=False):
             toff.append(len(paulis))
             coefs.append(coef)
         hoff.append(len(coefs))
-    ga = _gate_array(gates) if gates else None
-    pa = np.ascontiguousarray(paulis if paulis else [0], dtype=np.uint8)
-    qa = np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp)
-    ta = np.ascontiguousarray(toff, dtype=np.uintp)
-    ca = np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64)
-    ha = np.ascontiguousarray(hoff, dtype=np.uintp)
-    e = np.zeros(max(len(circuits), 1), np.float64)
+    return {"n": len(circuits), "nq": nq, "gates": _gate_array(gates) if gates else None, "goff": goff,
+            "paulis": np.ascontiguousarray(paulis if paulis else [0], dtype=np.uint8),
+            "qubits": np.ascontiguousarray(qubits if qubits else [0], dtype=np.uintp),
+            "toff": np.ascontiguousarray(toff, dtype=np.uintp),
+            "coefs": np.ascontiguousarray(coefs if coefs else [0.0], dtype=np.float64),
+            "hoff": np.ascontiguousarray(hoff, dtype=np.uintp)}
+
+
+def batch_circuits_run(packed, prec="c64", fast_c128=False):
+    """One kbwg_batch_circuits_exp_value call on prepared arrays."""
+    e = np.zeros(max(packed["n"], 1), np.float64)
     N.check(N.load().kbwg_batch_circuits_exp_value(
-        len(circuits), _DT[prec][0], N.FLAG_FAST_C128 if fast_c128 else 0, _p(nq, ctypes.c_uint32), ga,
-        _p(goff, ctypes.c_size_t), _p(pa, ctypes.c_uint8), _p(qa, ctypes.c_size_t), _p(ta, ctypes.c_size_t),
-        _p(ca, ctypes.c_double), _p(ha, ctypes.c_size_t), _p(e, ctypes.c_double)))
-    return e[: len(circuits)]
+        packed["n"], _DT[prec][0], N.FLAG_FAST_C128 if fast_c128 else 0, _p(packed["nq"], ctypes.c_uint32),
+        packed["gates"], _p(packed["goff"], ctypes.c_size_t), _p(packed["paulis"], ctypes.c_uint8),
+        _p(packed["qubits"], ctypes.c_size_t), _p(packed["toff"], ctypes.c_size_t),
+        _p(packed["coefs"], ctypes.c_double), _p(packed["hoff"], ctypes.c_size_t), _p(e, ctypes.c_double)))
+    return e[: packed["n"]]
+
+
+def batch_circuits_exp_value(circuits, prec="c64", fast_c128=False):
+    """<H> of many circuits in one launch: circuits is a list of
+    (num_qubits, gate list, hamiltonian); returns one energy per circuit."""
+    return batch_circuits_run(batch_circuits_prepare(circuits), prec, fast_c128)
 
 
 def batch_release():
