@@ -21,6 +21,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "../../include/kbwg.h"
@@ -40,7 +43,7 @@ struct BatchSweep {
 
 struct BatchJob {
     uint32_t n, nsweeps, sweep_off, nterms;
-    uint32_t term_off, id;
+    uint32_t term_off, id, pad;
 };
 
 struct BatchTerm {
@@ -258,11 +261,32 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
 struct BatchCircuitIn {
     uint32_t n;
     std::vector<GateDesc> gates;
-    std::vector<BatchTerm> terms;
+    std::vector<BatchTerm> terms;  // sorted by flip mask
+    // the circuit's plan (batch_run)
+    std::vector<BatchSweep> sweeps;
+    std::vector<TileGate> prog;
+    bool placed = true;
+    // validation result
+    int32_t status = KBWG_OK;
+    const char *error = nullptr;
 };
 
+// fn(i) for i in [0, n) on all host cores (items taken one at a time)
+template <class F>
+static void batch_parallel_for(size_t n, F &&fn) {
+    const size_t nt = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i; (i = next.fetch_add(1, std::memory_order_relaxed)) < n;) fn(i);
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(worker);
+    worker();
+    for (std::thread &t : pool) t.join();
+}
+
 template <class P, int K, int R>
-static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, double *energies) {
+static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *energies) {
     using BK = BatchKernel<P, K, R>;
     using Mem = typename P::Mem;
     auto fail = [](cudaError_t e, const char *what) {
@@ -272,23 +296,13 @@ static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, dou
         return e == cudaErrorMemoryAllocation ? (int32_t)KBWG_ENOMEM : (int32_t)KBWG_ECUDA;
     };
     (void)prec;
-    std::vector<BatchJob> jobs;
-    std::vector<BatchSweep> sweeps;
-    std::vector<TileGate> prog;
-    std::vector<BatchTerm> terms;
-    uint32_t nmax = 0;
-    for (size_t c = 0; c < circs.size(); c++) {
-        const BatchCircuitIn &ci = circs[c];
+    // plan every circuit (in parallel: the circuits are independent)
+    batch_parallel_for(circs.size(), [&](size_t c) {
+        BatchCircuitIn &ci = circs[c];
         const uint32_t nplan = std::max<uint32_t>(ci.n, (uint32_t)K);  // small registers padded with |0> qubits
         const std::vector<PlannedSweep> plan =
             plan_sweeps(nplan, K, R, ci.gates.data(), ci.gates.size(), false, kMaxSweepGates);
         size_t placed = 0;
-        BatchJob j;
-        memset(&j, 0, sizeof j);
-        j.n = ci.n;
-        j.id = (uint32_t)c;
-        j.sweep_off = (uint32_t)sweeps.size();
-        j.nsweeps = (uint32_t)plan.size();
         for (const PlannedSweep &sw : plan) {
             BatchSweep b;
             memset(&b, 0, sizeof b);
@@ -297,30 +311,65 @@ static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, dou
             memcpy(b.hq, sw.hq, sizeof b.hq);
             b.nstages = (uint32_t)sw.stage_layout.size();
             b.gate_count = (uint32_t)sw.gates.size();
-            b.gate_off = (uint32_t)prog.size();
+            b.gate_off = (uint32_t)ci.prog.size();  // within the circuit; rebased below
             for (uint32_t i = 0; i < b.nstages; i++) {
                 b.stage_layout[i] = sw.stage_layout[i];
                 b.stage_end[i] = sw.stage_end[i];
             }
             for (TileGate t : sw.gates) {
                 P::pack_host(t);
-                prog.push_back(t);
+                ci.prog.push_back(t);
             }
             placed += sw.gates.size();
-            sweeps.push_back(b);
+            ci.sweeps.push_back(b);
         }
-        if (placed != ci.gates.size()) {
+        ci.placed = placed == ci.gates.size();
+    });
+    // lay the programs out one after another: offsets first, then the copies
+    // (in parallel again) into arrays sized once
+    std::vector<BatchJob> jobs(circs.size());
+    size_t nsweeps = 0, nprog = 0, nterms = 0;
+    uint32_t nmax = 0;
+    for (size_t c = 0; c < circs.size(); c++) {
+        const BatchCircuitIn &ci = circs[c];
+        if (!ci.placed) {
             set_error(KBWG_EINVAL, "batch circuits: the planner could not place a circuit's gates");
             return KBWG_EINVAL;
         }
-        j.term_off = (uint32_t)terms.size();
+        BatchJob &j = jobs[c];
+        memset(&j, 0, sizeof j);
+        j.n = ci.n;
+        j.id = (uint32_t)c;
+        j.sweep_off = (uint32_t)nsweeps;
+        j.nsweeps = (uint32_t)ci.sweeps.size();
+        j.term_off = (uint32_t)nterms;
         j.nterms = (uint32_t)ci.terms.size();
-        std::vector<BatchTerm> t = ci.terms;
-        std::stable_sort(t.begin(), t.end(), [](const BatchTerm &x, const BatchTerm &y) { return x.x < y.x; });
-        terms.insert(terms.end(), t.begin(), t.end());
-        jobs.push_back(j);
+        j.pad = (uint32_t)nprog;  // the circuit's first gate, for the copies below
+        nsweeps += ci.sweeps.size();
+        nprog += ci.prog.size();
+        nterms += ci.terms.size();
         nmax = std::max(nmax, ci.n);
     }
+    if (nprog > UINT32_MAX || nsweeps > UINT32_MAX || nterms > UINT32_MAX) {
+        set_error(KBWG_EINVAL, "batch circuits: more than 2^32 planned gates, sweeps or strings");
+        return KBWG_EINVAL;
+    }
+    std::unique_ptr<BatchSweep[]> sweeps(new BatchSweep[std::max<size_t>(nsweeps, 1)]);
+    std::unique_ptr<TileGate[]> prog(new TileGate[std::max<size_t>(nprog, 1)]);
+    std::unique_ptr<BatchTerm[]> terms(new BatchTerm[std::max<size_t>(nterms, 1)]);
+    batch_parallel_for(circs.size(), [&](size_t c) {
+        BatchCircuitIn &ci = circs[c];
+        BatchJob &j = jobs[c];
+        const uint32_t base = j.pad;
+        j.pad = 0;
+        for (size_t i = 0; i < ci.sweeps.size(); i++) {
+            BatchSweep b = ci.sweeps[i];
+            b.gate_off += base;
+            sweeps[j.sweep_off + i] = b;
+        }
+        if (!ci.prog.empty()) memcpy(&prog[base], ci.prog.data(), ci.prog.size() * sizeof(TileGate));
+        if (!ci.terms.empty()) memcpy(&terms[j.term_off], ci.terms.data(), ci.terms.size() * sizeof(BatchTerm));
+    });
     // largest first: the persistent CTAs then finish together
     std::stable_sort(jobs.begin(), jobs.end(), [&](const BatchJob &x, const BatchJob &y) {
         const double cx = (double)(1ull << x.n) * (1.0 + x.nsweeps + 0.25 * x.nterms);
@@ -338,9 +387,9 @@ static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, dou
     const uint32_t grid = (uint32_t)std::min<size_t>(jobs.size(), (size_t)sms * std::max(occ, 1));
     const uint64_t slot_elems = nmax > (uint32_t)K ? (1ull << nmax) : 0;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t jb = jobs.size() * sizeof(BatchJob), swb = std::max<size_t>(sweeps.size(), 1) * sizeof(BatchSweep),
-                 pb = std::max<size_t>(prog.size(), 1) * sizeof(TileGate),
-                 tb = std::max<size_t>(terms.size(), 1) * sizeof(BatchTerm), eb = circs.size() * sizeof(double),
+    const size_t jb = jobs.size() * sizeof(BatchJob), swb = std::max<size_t>(nsweeps, 1) * sizeof(BatchSweep),
+                 pb = std::max<size_t>(nprog, 1) * sizeof(TileGate),
+                 tb = std::max<size_t>(nterms, 1) * sizeof(BatchTerm), eb = circs.size() * sizeof(double),
                  sb = (size_t)grid * slot_elems * sizeof(Mem);
     const size_t o_sw = up(jb), o_p = o_sw + up(swb), o_t = o_p + up(pb), o_e = o_t + up(tb), o_c = o_e + up(eb),
                  o_err = o_c + 256, o_s = o_err + 256;
@@ -367,12 +416,12 @@ static int32_t batch_run(int prec, const std::vector<BatchCircuitIn> &circs, dou
     a.err = (int *)(dbuf + o_err);
     int err_flag = 0;
     e = copy_async(dbuf, jobs.data(), jb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !sweeps.empty())
-        e = copy_async(dbuf + o_sw, sweeps.data(), sweeps.size() * sizeof(BatchSweep), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !prog.empty())
-        e = copy_async(dbuf + o_p, prog.data(), prog.size() * sizeof(TileGate), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !terms.empty())
-        e = copy_async(dbuf + o_t, terms.data(), terms.size() * sizeof(BatchTerm), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nsweeps)
+        e = copy_async(dbuf + o_sw, sweeps.get(), nsweeps * sizeof(BatchSweep), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nprog)
+        e = copy_async(dbuf + o_p, prog.get(), nprog * sizeof(TileGate), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nterms)
+        e = copy_async(dbuf + o_t, terms.get(), nterms * sizeof(BatchTerm), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dbuf + o_c, 0, 512, st);
     if (e == cudaSuccess) {
         k_batch_circuits<P, K, R><<<grid, BK::kThreads, BK::kSmem, st>>>(a);
@@ -399,40 +448,35 @@ int32_t batch_circuits(int precision, uint32_t flags, size_t ncirc, const uint32
                        const uintptr_t *term_offsets, const double *coefficients, const uintptr_t *ham_offsets,
                        double *energies) {
     std::vector<BatchCircuitIn> circs(ncirc);
-    for (size_t c = 0; c < ncirc; c++) {
+    batch_parallel_for(ncirc, [&](size_t c) {
         BatchCircuitIn &ci = circs[c];
+        auto bad = [&](int32_t code, const char *msg) {
+            ci.status = code;
+            ci.error = msg;
+        };
         const uint32_t n = num_qubits[c];
-        if (n < 1 || n > kBatchMaxQubits) {
-            set_error(KBWG_EQUBITS, "batch circuits: every circuit needs 1..24 qubits");
-            return KBWG_EQUBITS;
-        }
+        if (n < 1 || n > kBatchMaxQubits) return bad(KBWG_EQUBITS, "batch circuits: every circuit needs 1..24 qubits");
         ci.n = n;
-        if (gate_offsets[c + 1] < gate_offsets[c] || ham_offsets[c + 1] < ham_offsets[c]) {
-            set_error(KBWG_EINVAL, "batch circuits: offsets must not decrease");
-            return KBWG_EINVAL;
-        }
+        if (gate_offsets[c + 1] < gate_offsets[c] || ham_offsets[c + 1] < ham_offsets[c])
+            return bad(KBWG_EINVAL, "batch circuits: offsets must not decrease");
+        ci.gates.reserve(gate_offsets[c + 1] - gate_offsets[c]);
         for (uintptr_t i = gate_offsets[c]; i < gate_offsets[c + 1]; i++) {
             const kbwg_gate &g = gates[i];
-            if (g.kind > KBWG_RZ || g.target >= n || (g.control_mask >> n) || (g.control_mask & (1ull << g.target))) {
-                set_error(KBWG_EINVAL, "batch circuits: bad gate (kind, target or controls)");
-                return KBWG_EINVAL;
-            }
+            if (g.kind > KBWG_RZ || g.target >= n || (g.control_mask >> n) || (g.control_mask & (1ull << g.target)))
+                return bad(KBWG_EINVAL, "batch circuits: bad gate (kind, target or controls)");
             ci.gates.push_back(make_gate_desc(precision, g.kind, g.target, g.control_mask, g.angle));
         }
+        ci.terms.reserve(ham_offsets[c + 1] - ham_offsets[c]);
         for (uintptr_t k = ham_offsets[c]; k < ham_offsets[c + 1]; k++) {
             BatchTerm t;
             memset(&t, 0, sizeof t);
             int ny = 0;
+            if (term_offsets[k + 1] < term_offsets[k]) return bad(KBWG_EINVAL, "batch circuits: offsets must not decrease");
             for (uintptr_t i = term_offsets[k]; i < term_offsets[k + 1]; i++) {
-                if (qubits[i] >= n || paulis[i] < 1 || paulis[i] > 3) {
-                    set_error(KBWG_EINVAL, "batch circuits: bad Pauli code or qubit");
-                    return KBWG_EINVAL;
-                }
+                if (qubits[i] >= n || paulis[i] < 1 || paulis[i] > 3)
+                    return bad(KBWG_EINVAL, "batch circuits: bad Pauli code or qubit");
                 const uint64_t b = 1ull << qubits[i];
-                if ((t.x | t.z) & b) {
-                    set_error(KBWG_EINVAL, "batch circuits: a string names a qubit twice");
-                    return KBWG_EINVAL;
-                }
+                if ((t.x | t.z) & b) return bad(KBWG_EINVAL, "batch circuits: a string names a qubit twice");
                 if (paulis[i] == 1) t.x |= b;
                 else if (paulis[i] == 2) t.x |= b, t.z |= b, ny++;
                 else t.z |= b;
@@ -442,7 +486,14 @@ int32_t batch_circuits(int precision, uint32_t flags, size_t ncirc, const uint32
             t.ci = coefficients[k] * im[ny & 3];
             ci.terms.push_back(t);
         }
-    }
+        std::stable_sort(ci.terms.begin(), ci.terms.end(),
+                         [](const BatchTerm &x, const BatchTerm &y) { return x.x < y.x; });
+    });
+    for (const BatchCircuitIn &ci : circs)  // the first bad circuit's error
+        if (ci.status != KBWG_OK) {
+            set_error(ci.status, ci.error);
+            return ci.status;
+        }
     if (ncirc == 0) return KBWG_OK;
     if (precision == KBWG_C64) return batch_run<FastP, 12, 4>(precision, circs, energies);
     if (flags & KBWG_FLAG_FAST_C128) return batch_run<FF2B, 11, 3>(precision, circs, energies);
