@@ -158,8 +158,11 @@ def cpu_port_rate(n, prec, gates, budget_s, threads=None):
 
 def run_reference(args, world, rank):
     """The reference's CPU Dense path, as the oracle port (the Rust crate
-    cannot be built here): each step applies a bounded slice of the same
-    brickwork circuit at 30 qubits with every host thread."""
+    cannot be built here), with every host thread, on the 30-qubit brickwork.
+    By default the timed steps apply the whole circuit once between them
+    (step s: the s-th of `steps` contiguous chunks, so every layer and the
+    CNOT mix are in the rate); each warm-up step applies 4 gates.
+    --ref-gates G instead applies G consecutive gates per step."""
     if rank != 0:
         return
     from kbw_gb300 import circuits as C
@@ -168,33 +171,41 @@ def run_reference(args, world, rank):
     circ = C.brickwork(n, args.layers, 0)
     o = oracle.OracleDense(n, prec)
     B = 16 if prec == "c128" else 8
-    per_step = args.ref_gates
     pos = 0
 
-    def step():
+    def apply(count):
         nonlocal pos
-        for _ in range(per_step):
+        for _ in range(count):
             kind, t, c, a = circ[pos % len(circ)]
             o.gate(kind, t, c, a)
             pos += 1
 
     for _ in range(args.warmup):
-        step()
+        apply(args.ref_gates or 4)
+    if args.ref_gates:
+        chunks = [args.ref_gates] * args.steps
+    else:
+        pos = 0
+        chunks = [(s + 1) * len(circ) // args.steps - s * len(circ) // args.steps for s in range(args.steps)]
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
+    for cnt in chunks:
+        apply(cnt)
     dt = time.perf_counter() - t0
-    value = args.steps * per_step * 2 * B * (1 << n) / dt / 1e9
+    total = sum(chunks)
+    per_step = total / args.steps
+    value = total * 2 * B * (1 << n) / dt / 1e9
+    sample = ("%d gates per step of the %dq brickwork" % (args.ref_gates, n) if args.ref_gates else
+              "the whole %dq brickwork (%d gates) once across the timed steps" % (n, total))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "c128" else "f32", "data": "synthetic",
         "config": {"workload": "brickwork-%dq-%dlayers-%s" % (n, args.layers, prec), "qubits": n,
-                   "precision": prec, "gates_per_step": per_step},
+                   "layers": args.layers, "gates": len(circ), "precision": prec},
+        "gates_per_step": round(per_step, 2),
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
-                         "sample": "%d gates per step of the %dq brickwork, restated Dense<f64> (OpenMP)"
-                                   % (per_step, n)},
+                         "sample": sample + ", restated Dense<f64> (OpenMP)"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -384,9 +395,11 @@ def run_grover_bench(args, torch, DenseGB300, C):
 def run_gate_classes(args):
     """Per gate class: CUDA-event time of the sweeps that apply 32 gates of
     one class (first row: a single RZ, the memory-pass floor of a sweep);
-    us_per_gate = sweep time / gates.  Runs of diagonal gates are not folded
-    here, so each of the 32 gates is applied."""
+    us_per_gate = sweep time / gates, once with the interpreted sweep kernel
+    and once with the sweep's run-time-specialised kernel.  Runs of diagonal
+    gates are not folded here, so each of the 32 gates is applied."""
     from kbw_gb300 import DenseGB300
+    from kbw_gb300 import _native as N
     from kbw_gb300 import circuits as C
     n, prec = args.qubits, args.prec
     sim = DenseGB300(n, prec, fast_c128=(prec == "c128" and args.arith == "ff"), fold=False)
@@ -403,16 +416,22 @@ def run_gate_classes(args):
              ("brickwork 13 qubits, 3 layers", C.brickwork(13, 3, 0))]
     out = []
     for name, circ in cases:
-        sim.apply(circ)
-        sim.flush()
-        sim.profile(True)
-        for _ in range(3):
+        row = {"case": name, "gates": len(circ)}
+        for mode, jit in (("interpreted", N.JIT_OFF), ("specialised", N.JIT_ALWAYS)):
+            sim.set_jit(jit)
             sim.apply(circ)
             sim.flush()
-        nl, ms, b = sim.profile_read()
-        sim.profile(False)
-        out.append({"case": name, "gates": len(circ), "sweeps": nl // 3, "ms_per_rep": round(ms / 3, 4),
-                    "us_per_gate": round(1000 * ms / 3 / len(circ), 3)})
+            sim.jit_wait()
+            sim.profile(True)
+            for _ in range(3):
+                sim.apply(circ)
+                sim.flush()
+            nl, ms, b = sim.profile_read()
+            sim.profile(False)
+            row["sweeps"] = nl // 3
+            row[mode] = {"ms_per_rep": round(ms / 3, 4), "us_per_gate": round(1000 * ms / 3 / len(circ), 3),
+                         "specialised_sweeps": sim.jit_info()["last_specialised"]}
+        out.append(row)
     sim.close()
     return out
 
@@ -871,7 +890,8 @@ def main():
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="keep the default tile size and fusion depth instead of autotuning them")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-gates", type=int, default=4)
+    ap.add_argument("--ref-gates", type=int, default=0,
+                    help="reference arm: gates per step (0: the whole circuit across the timed steps)")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     ap.add_argument("--no-batch", dest="batch", action="store_false")
