@@ -175,7 +175,9 @@ int32_t kbwg_exp_value(kbwg_sim *sim, const uint8_t *paulis, const uintptr_t *qu
  * Hamiltonian is given as in kbwg_exp_value.  Up to max_checkpoints copies of
  * the forward state (as memory allows) bound the uncompute drift.  Writes E
  * and gradient[n_params]; the handle is left in |0...0>.  Needs >= 12 qubits
- * (complex64) or >= 11 (complex128). */
+ * (complex64) or >= 11 (complex128).  The call's scratch (lambda and the
+ * checkpoints) stays with the handle for the next call while it takes at most
+ * a sixteenth of the device's memory, and is freed by kbwg_free. */
 int32_t kbwg_adjoint_gradient(kbwg_sim *sim, const kbwg_gate *gates, uintptr_t n_gates,
                               const int32_t *param_index, uintptr_t n_params, const uint8_t *paulis,
                               const uintptr_t *qubits, const uintptr_t *offsets, const double *coefficients,

@@ -356,27 +356,68 @@ __global__ void k_sum_slots(const double *partials, uint32_t nblocks, uint32_t n
 }
 
 // ---- host orchestration ----------------------------------------------------------------
-struct AdjBuffers {
+// Scratch of the adjoint gradient, kept with the handle between calls:
+// lambda, the checkpoints (both only while they are small against the
+// device, see adjoint_run), the per-block partials, the gradient, the
+// programs and gradient info of every reverse sweep (device, and a pinned
+// staging copy uploaded once per call), and the specialised reverse-sweep
+// kernels of each segment structure seen.
+struct AdjScratch {
+    size_t sb = 0;  // state bytes lam/ckpt were made for
     void *lam = nullptr;
     std::vector<void *> ckpt;
     double *partials = nullptr;
+    size_t partials_cap = 0;
     double *grads = nullptr;
-    uint32_t *meta = nullptr;  // ginfo + gate_of_slot
-    void *prog = nullptr;
-    void release() {
+    size_t grads_cap = 0;
+    unsigned char *dprog = nullptr;
+    size_t dprog_cap = 0;
+    unsigned char *hprog = nullptr;  // pinned
+    size_t hprog_cap = 0;
+    struct Kernels {
+        uint64_t key;
+        std::vector<const void *> f;
+    };
+    std::vector<Kernels> kernels;  // final entries only (compiled, loaded or failed)
+    void release_states() {
         if (lam) cudaFree(lam);
+        lam = nullptr;
         for (void *c : ckpt) cudaFree(c);
         ckpt.clear();
+        sb = 0;
+    }
+    void release() {
+        release_states();
         if (partials) cudaFree(partials);
         if (grads) cudaFree(grads);
-        if (meta) cudaFree(meta);
-        if (prog) cudaFree(prog);
-        lam = nullptr;
+        if (dprog) cudaFree(dprog);
+        if (hprog) cudaFreeHost(hprog);
         partials = grads = nullptr;
-        meta = nullptr;
-        prog = nullptr;
+        dprog = hprog = nullptr;
+        partials_cap = grads_cap = dprog_cap = hprog_cap = 0;
+        kernels.clear();
     }
 };
+constexpr size_t kAdjKernelEntries = 256;
+
+void release_adjoint(Sim &s) {
+    AdjScratch *a = (AdjScratch *)s.adj;
+    if (!a) return;
+    a->release();
+    delete a;
+    s.adj = nullptr;
+}
+
+template <class B>
+static cudaError_t adj_grow(B *&p, size_t &cap, size_t want) {
+    if (want <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMalloc((void **)&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+}
 
 static GateDesc inverse_desc(int prec, const GateDesc &g, double angle) {
     // X, Y, Z, H are their own inverses; P/RX/RY/RZ invert by negating the angle
@@ -389,120 +430,162 @@ static GateDesc inverse_desc(int prec, const GateDesc &g, double angle) {
     }
 }
 
-template <class P, int K, int R>
-static cudaError_t adjoint_segment(Sim &s, AdjBuffers &bufs, const std::vector<GateDesc> &fwd,
-                                   const std::vector<double> &angles, const std::vector<int> &gtype, size_t lo,
-                                   size_t hi, int num_sms) {
-    using AK = AdjKernel<P, K, R>;
-    using Mem = typename P::Mem;
-    {
-        const cudaError_t e = ensure_smem_limit((const void *)k_adjoint<P, K, R>, AK::kSmem);
-        if (e != cudaSuccess) return e;
+// One reverse sweep, planned: its parameters (program and gradient info
+// pointers filled once the upload buffer exists), the byte offsets of its
+// program and info in that buffer, and its specialised kernel (or null).
+struct RevSweep {
+    AdjParams a;
+    size_t prog_off = 0, info_off = 0;
+    const void *spec = nullptr;
+};
+
+static uint64_t fnv(uint64_t h, const void *p, size_t n) {
+    const unsigned char *c = (const unsigned char *)p;
+    for (size_t i = 0; i < n; i++) {
+        h ^= c[i];
+        h *= 1099511628211ull;
     }
-    // reverse list of inverse gates; gradient info follows each gate through the planner
+    return h;
+}
+
+// Plan the reverse sweeps of gates [lo, hi) (inverse gates, last first),
+// append their programs and gradient info to the staging bytes, and find
+// their specialised kernels (from the handle's cache, else following the
+// JIT mode).
+template <class P, int K, int R>
+static cudaError_t plan_segment(Sim &s, AdjScratch &sc, const std::vector<GateDesc> &fwd,
+                                const std::vector<double> &angles, const std::vector<int> &gtype, size_t lo, size_t hi,
+                                std::vector<unsigned char> &progs, std::vector<unsigned char> &infos,
+                                std::vector<RevSweep> &out) {
+    using AK = AdjKernel<P, K, R>;
     std::vector<GateDesc> rev;
     std::vector<size_t> rev_src;
     for (size_t j = hi; j-- > lo;) {
         rev.push_back(inverse_desc(s.prec, fwd[j], angles[j]));
         rev_src.push_back(j);
     }
-    std::vector<PlannedSweep> plan = plan_sweeps(s.n, K, R, rev.data(), rev.size(), false);
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<P, K, R>, AK::kThreads, AK::kSmem);
-    if (e != cudaSuccess) return e;
-    const uint64_t tiles = 1ull << (s.n - K);
-    // gradient info per sweep: type | slot << 4 per gate, and the gate of each slot
+    const std::vector<PlannedSweep> plan = plan_sweeps(s.n, K, R, rev.data(), rev.size(), false);
+    // gradient info per sweep: type | slot << 4 per gate, then the gate of each slot
     std::vector<std::vector<uint32_t>> metas(plan.size());
-    std::vector<uint32_t> slots(plan.size(), 0);
+    uint64_t key = fnv(1469598103934665603ull, AdjPolicyName<P>::s, strlen(AdjPolicyName<P>::s));
+    const size_t first = out.size();
     for (size_t k = 0; k < plan.size(); k++) {
         const PlannedSweep &sw = plan[k];
         std::vector<uint32_t> &meta = metas[k];
-        meta.assign(2 * kMaxSweepGates, 0);
-        uint32_t nslots = 0;
+        meta.assign(sw.gates.size(), 0);
+        std::vector<uint32_t> gate_of_slot;
         for (size_t i = 0; i < sw.gates.size(); i++) {
             const size_t j = rev_src[sw.src[i]];
             if (gtype[j] != GT_NONE) {
-                meta[i] = (uint32_t)gtype[j] | (nslots << 4);
-                meta[kMaxSweepGates + nslots] = (uint32_t)j;
-                nslots++;
+                meta[i] = (uint32_t)gtype[j] | ((uint32_t)gate_of_slot.size() << 4);
+                gate_of_slot.push_back((uint32_t)j);
             }
         }
-        slots[k] = nslots;
-    }
-    // run-time specialised reverse sweeps (the handle's JIT mode, as for the
-    // forward sweeps); a sweep without one runs the compiled k_adjoint
-    std::vector<const void *> jk;
-    if (s.jit_mode != KBWG_JIT_OFF) {
-        const JitGeometry geo{AdjPolicyName<P>::s, K, R, AK::kThreads, 2};
-        std::vector<std::string> srcs;
-        for (size_t k = 0; k < plan.size(); k++) srcs.push_back(jit_adjoint_source(geo, plan[k], metas[k]));
-        jk = specialised_kernels(s, srcs, "kbwg_jit_adjoint");
-        for (const void *f : jk) {
-            if (!f) continue;
-            e = ensure_smem_limit(f, AK::kSmem);
-            if (e != cudaSuccess) return e;
-            int o = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, f, AK::kThreads, AK::kSmem);
-            if (e != cudaSuccess) return e;
-            occ = std::min(occ, std::max(o, 1));  // one grid size for both kernels (partials buffer)
+        RevSweep r;
+        memset(&r.a, 0, sizeof r.a);
+        r.a.sw.hmask = sw.hmask;
+        r.a.sw.l = sw.l;
+        r.a.sw.m = sw.m;
+        memcpy(r.a.sw.hq, sw.hq, sizeof r.a.sw.hq);
+        r.a.sw.nstages = (uint32_t)sw.stage_layout.size();
+        r.a.sw.gate_count = (uint32_t)sw.gates.size();
+        for (uint32_t i = 0; i < r.a.sw.nstages; i++) {
+            r.a.sw.stage_layout[i] = sw.stage_layout[i];
+            r.a.sw.stage_end[i] = sw.stage_end[i];
         }
+        r.a.sw.err = s.d_err;
+        r.a.sw.tiles = 1ull << (s.n - K);
+        r.a.nslots = (uint32_t)gate_of_slot.size();
+        // structure key: everything the specialised source is written from
+        key = fnv(key, &r.a.sw.l, sizeof r.a.sw.l);
+        key = fnv(key, &r.a.sw.m, sizeof r.a.sw.m);
+        key = fnv(key, sw.hq, sizeof sw.hq);
+        key = fnv(key, sw.stage_layout.data(), sw.stage_layout.size());
+        key = fnv(key, sw.stage_end.data(), sw.stage_end.size() * sizeof(uint16_t));
+        key = fnv(key, meta.data(), meta.size() * sizeof(uint32_t));
+        for (const TileGate &t : sw.gates) {
+            key = fnv(key, &t, offsetof(TileGate, c));
+            if (t.cls == TG_PI) key = fnv(key, &t.c[0], sizeof(double));
+        }
+        key = fnv(key, "|", 1);
+        // program (policy-packed constants) and gradient info into the staging bytes
+        r.prog_off = progs.size();
+        progs.resize(progs.size() + sw.gates.size() * sizeof(TileGate));
+        for (size_t i = 0; i < sw.gates.size(); i++) {
+            TileGate t = sw.gates[i];
+            P::pack_host(t);
+            memcpy(progs.data() + r.prog_off + i * sizeof(TileGate), &t, sizeof t);
+        }
+        r.info_off = infos.size();
+        const size_t nb = (meta.size() + gate_of_slot.size()) * sizeof(uint32_t);
+        infos.resize(infos.size() + ((nb + 15) & ~(size_t)15));
+        if (!meta.empty()) memcpy(infos.data() + r.info_off, meta.data(), meta.size() * sizeof(uint32_t));
+        if (!gate_of_slot.empty())
+            memcpy(infos.data() + r.info_off + meta.size() * sizeof(uint32_t), gate_of_slot.data(),
+                   gate_of_slot.size() * sizeof(uint32_t));
+        out.push_back(r);
     }
-    const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)num_sms * std::max(occ, 1));
+    // specialised reverse sweeps (the handle's JIT mode, as for the forward
+    // sweeps); a sweep without one runs the compiled k_adjoint
+    if (s.jit_mode == KBWG_JIT_OFF) return cudaSuccess;
+    key = fnv(key, &s.jit_mode, sizeof s.jit_mode);
+    for (const AdjScratch::Kernels &kc : sc.kernels)
+        if (kc.key == key && kc.f.size() == plan.size()) {
+            for (size_t k = 0; k < plan.size(); k++) out[first + k].spec = kc.f[k];
+            return cudaSuccess;
+        }
+    const JitGeometry geo{AdjPolicyName<P>::s, K, R, AK::kThreads, 2};
+    std::vector<std::string> srcs;
+    for (size_t k = 0; k < plan.size(); k++) srcs.push_back(jit_adjoint_source(geo, plan[k], metas[k]));
+    bool final = false;
+    const std::vector<const void *> jk = specialised_kernels(s, srcs, "kbwg_jit_adjoint", &final);
     for (size_t k = 0; k < plan.size(); k++) {
-        const PlannedSweep &sw = plan[k];
-        const size_t ng = sw.gates.size();
-        std::vector<TileGate> prog = sw.gates;
-        for (TileGate &t : prog) P::pack_host(t);
-        const std::vector<uint32_t> &meta = metas[k];
-        const uint32_t nslots = slots[k];
-        e = copy_async(bufs.prog, prog.data(), ng * sizeof(TileGate), cudaMemcpyHostToDevice, s.stream);
+        const void *f = jk.empty() ? nullptr : jk[k];
+        if (!f) continue;
+        cudaError_t e = ensure_smem_limit(f, AK::kSmem);
         if (e != cudaSuccess) return e;
-        e = copy_async(bufs.meta, meta.data(), meta.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s.stream);
-        if (e != cudaSuccess) return e;
-        AdjParams a;
-        memset(&a, 0, sizeof a);
-        a.sw.hmask = sw.hmask;
-        a.sw.l = sw.l;
-        a.sw.m = sw.m;
-        memcpy(a.sw.hq, sw.hq, sizeof a.sw.hq);
-        a.sw.nstages = (uint32_t)sw.stage_layout.size();
-        a.sw.gate_count = (uint32_t)ng;
-        for (uint32_t i = 0; i < a.sw.nstages; i++) {
-            a.sw.stage_layout[i] = sw.stage_layout[i];
-            a.sw.stage_end[i] = sw.stage_end[i];
-        }
-        a.sw.prog = (const TileGate *)bufs.prog;
-        a.sw.err = s.d_err;
-        a.sw.tiles = tiles;
-        a.ginfo = bufs.meta;
-        a.partials = bufs.partials;
-        a.nslots = nslots;
+        out[first + k].spec = f;
+    }
+    if (final) {
+        if (sc.kernels.size() >= kAdjKernelEntries) sc.kernels.erase(sc.kernels.begin());
+        sc.kernels.push_back({key, jk});
+    }
+    return cudaSuccess;
+}
+
+// Launch the planned reverse sweeps of one segment (programs already uploaded).
+template <class P, int K, int R>
+static cudaError_t run_segment(Sim &s, AdjScratch &sc, std::vector<RevSweep> &sweeps,
+                               const std::vector<uint64_t> &grids, size_t from, size_t to) {
+    using AK = AdjKernel<P, K, R>;
+    using Mem = typename P::Mem;
+    for (size_t k = from; k < to; k++) {
+        RevSweep &r = sweeps[k];
+        const uint64_t grid = grids[k];
         if (s.prof.on) s.prof.mark(s.stream);
-        const void *spec = jk.empty() ? nullptr : jk[k];
-        if (spec) {
-            Mem *ph = (Mem *)s.state, *la = (Mem *)bufs.lam;
-            void *args[] = {(void *)&ph, (void *)&la, (void *)&a};
-            cudaLaunchKernel(spec, dim3((unsigned)grid), dim3(AK::kThreads), args, AK::kSmem, s.stream);
+        cudaError_t e;
+        if (r.spec) {
+            Mem *ph = (Mem *)s.state, *la = (Mem *)sc.lam;
+            void *args[] = {(void *)&ph, (void *)&la, (void *)&r.a};
+            e = cudaLaunchKernel(r.spec, dim3((unsigned)grid), dim3(AK::kThreads), args, AK::kSmem, s.stream);
         } else {
-            k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)bufs.lam,
-                                                                                    a);
+            k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)sc.lam,
+                                                                                    r.a);
+            e = cudaGetLastError();
         }
         count_launch();
-        e = cudaGetLastError();
         if (s.prof.on) {
             s.prof.mark(s.stream);
             s.prof.bytes += 4.0 * (double)s.elem * (double)s.ns;
         }
         if (e != cudaSuccess) return e;
-        if (nslots) {
-            k_sum_slots<<<(nslots + 3) / 4, 128, 0, s.stream>>>(bufs.partials, (uint32_t)grid, nslots,
-                                                                bufs.meta + kMaxSweepGates, bufs.grads);
+        if (r.a.nslots) {
+            k_sum_slots<<<(r.a.nslots + 3) / 4, 128, 0, s.stream>>>(sc.partials, (uint32_t)grid, r.a.nslots,
+                                                                    r.a.ginfo + r.a.sw.gate_count, sc.grads);
             count_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        // (the next sweep's uploads into prog/meta are stream-ordered after this
-        // sweep's kernels: no host synchronisation needed)
     }
     return cudaSuccess;
 }
@@ -570,18 +653,16 @@ static cudaError_t apply_hamiltonian(Sim &s, void *lam, const std::vector<ApplyG
     return cudaSuccess;
 }
 
+// Re<a|b> into the handle's pinned result slot; readable after the stream's
+// next synchronisation.
 template <class T>
-static cudaError_t inner_re(Sim &s, const void *a, const void *b, double *out) {
+static cudaError_t inner_re_async(Sim &s, const void *a, const void *b) {
     k_inner_re<T><<<kReduceBlocks, 256, 0, s.stream>>>((const cx<T> *)a, (const cx<T> *)b, s.ns, s.rs.partials,
                                                         s.rs.ticket, s.rs.result);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    e = copy_async(s.h_result, s.rs.result, sizeof(double), cudaMemcpyDeviceToHost, s.stream);
-    if (e != cudaSuccess) return e;
-    e = cudaStreamSynchronize(s.stream);
-    *out = s.h_result[0];
-    return e;
+    return copy_async(s.h_result, s.rs.result, sizeof(double), cudaMemcpyDeviceToHost, s.stream);
 }
 
 static std::vector<ApplyGroup> make_groups(const std::vector<PauliString> &H) {
@@ -619,9 +700,13 @@ template <class P, class T, int K, int R>
 static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
                            const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
                            std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
-    AdjBuffers bufs;
+    using AK = AdjKernel<P, K, R>;
+    if (!s.adj) s.adj = new AdjScratch();
+    AdjScratch &sc = *(AdjScratch *)s.adj;
     auto fail_cuda = [&](cudaError_t e, const char *what) {
-        bufs.release();
+        cudaGetLastError();
+        cudaStreamSynchronize(s.stream);
+        sc.release();  // (nothing of it is in flight any more)
         cudaGetLastError();
         set_error(e == cudaErrorMemoryAllocation ? KBWG_ENOMEM : KBWG_ECUDA,
                   std::string("adjoint: ") + what + ": " + cudaGetErrorString(e));
@@ -632,29 +717,34 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
     int dev = 0, num_sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = ensure_smem_limit((const void *)k_adjoint<P, K, R>, AK::kSmem);
     if (e != cudaSuccess) return fail_cuda(e, "device query");
-    e = cudaMalloc(&bufs.lam, sb);
-    if (e != cudaSuccess) return fail_cuda(e, "lambda buffer");
-    e = cudaMalloc((void **)&bufs.partials, (size_t)num_sms * 8 * kMaxSweepGates * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&bufs.grads, std::max<size_t>(M, 1) * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&bufs.meta, 2 * kMaxSweepGates * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&bufs.prog, kMaxSweepGates * sizeof(TileGate));
+    // scratch (kept from an earlier call when it is there)
+    if (sc.sb != sb) sc.release_states();
+    if (!sc.lam) {
+        e = cudaMalloc(&sc.lam, sb);
+        if (e != cudaSuccess) return fail_cuda(e, "lambda buffer");
+        sc.sb = sb;
+    }
+    e = adj_grow(sc.partials, sc.partials_cap, (size_t)num_sms * 8 * kMaxSweepGates * sizeof(double));
+    if (e == cudaSuccess) e = adj_grow(sc.grads, sc.grads_cap, std::max<size_t>(M, 1) * sizeof(double));
     if (e != cudaSuccess) return fail_cuda(e, "scratch");
-    // checkpoints: as many as fit in 80% of the free memory, at most max_ckpt
+    // checkpoints: at most max_ckpt, new ones only while they fit in 80% of
+    // the free memory
+    const size_t want = std::min<size_t>(max_ckpt, M > 1 ? M - 1 : 0);
     size_t free_b = 0, total_b = 0;
     e = cudaMemGetInfo(&free_b, &total_b);
     if (e != cudaSuccess) return fail_cuda(e, "memory query");
-    size_t nck = std::min<size_t>(max_ckpt, (size_t)(0.8 * (double)free_b) / sb);
-    nck = std::min<size_t>(nck, M > 1 ? M - 1 : 0);
-    for (size_t i = 0; i < nck; i++) {
+    while (sc.ckpt.size() < want && sb <= (size_t)(0.8 * (double)free_b)) {
         void *c = nullptr;
         if (cudaMalloc(&c, sb) != cudaSuccess) {
             cudaGetLastError();
             break;
         }
-        bufs.ckpt.push_back(c);
+        sc.ckpt.push_back(c);
+        free_b -= std::min(free_b, sb);
     }
-    const size_t S = bufs.ckpt.size() + 1;
+    const size_t S = std::min(want, sc.ckpt.size()) + 1;
     std::vector<size_t> b(S + 1);
     for (size_t i = 0; i <= S; i++) b[i] = i * M / S;
 
@@ -669,41 +759,98 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         if (seg + 1 < S) {
             // checkpoints are binary64 (the reverse sweeps read that form); a
             // float-float forward state stays float-float and is exported
-            e = s.ff_resident ? launch_ff_export(s.state, bufs.ckpt[seg], s.n, s.stream)
-                              : cudaMemcpyAsync(bufs.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
+            e = s.ff_resident ? launch_ff_export(s.state, sc.ckpt[seg], s.n, s.stream)
+                              : cudaMemcpyAsync(sc.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
             if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
         }
+    }
+    // plan every reverse sweep while the GPU runs the forward pass; their
+    // programs and gradient info go up in one copy from pinned memory
+    std::vector<unsigned char> progs, infos;
+    std::vector<RevSweep> sweeps;
+    std::vector<size_t> seg_first(S + 1, 0);
+    for (size_t seg = S; seg-- > 0;) {
+        seg_first[seg + 1] = sweeps.size();  // (segments run last first)
+        e = plan_segment<P, K, R>(s, sc, fwd, angles, gtype, b[seg], b[seg + 1], progs, infos, sweeps);
+        if (e != cudaSuccess) return fail_cuda(e, "reverse plan");
+    }
+    const size_t up = progs.size() + infos.size();
+    if (up > sc.hprog_cap) {
+        if (sc.hprog) cudaFreeHost(sc.hprog);
+        sc.hprog = nullptr;
+        sc.hprog_cap = 0;
+        e = cudaHostAlloc((void **)&sc.hprog, up, cudaHostAllocDefault);
+        if (e != cudaSuccess) return fail_cuda(e, "staging buffer");
+        sc.hprog_cap = up;
+    }
+    e = adj_grow(sc.dprog, sc.dprog_cap, std::max<size_t>(up, 16));
+    if (e != cudaSuccess) return fail_cuda(e, "program buffer");
+    if (up) {
+        memcpy(sc.hprog, progs.data(), progs.size());
+        if (!infos.empty()) memcpy(sc.hprog + progs.size(), infos.data(), infos.size());
+        e = copy_async(sc.dprog, sc.hprog, up, cudaMemcpyHostToDevice, s.stream);
+        if (e != cudaSuccess) return fail_cuda(e, "program upload");
+    }
+    // one grid per kernel: as many CTAs as fit (the partials buffer holds 8 per SM)
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<P, K, R>, AK::kThreads, AK::kSmem);
+    if (e != cudaSuccess) return fail_cuda(e, "occupancy");
+    const uint64_t tiles = 1ull << (s.n - K);
+    std::vector<std::pair<const void *, uint64_t>> grids;
+    auto grid_of = [&](const void *f) -> uint64_t {
+        for (const auto &g : grids)
+            if (g.first == f) return g.second;
+        int o = occ;
+        if (f && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, f, AK::kThreads, AK::kSmem) != cudaSuccess) {
+            cudaGetLastError();
+            o = occ;
+        }
+        const uint64_t g = std::min<uint64_t>(tiles, (uint64_t)num_sms * std::min(std::max(o, 1), 8));
+        grids.emplace_back(f, g);
+        return g;
+    };
+    std::vector<uint64_t> grid(sweeps.size());
+    for (size_t k = 0; k < sweeps.size(); k++) {
+        RevSweep &r = sweeps[k];
+        r.a.sw.prog = (const TileGate *)(sc.dprog + r.prog_off);
+        r.a.ginfo = (const uint32_t *)(sc.dprog + progs.size() + r.info_off);
+        r.a.partials = sc.partials;
+        grid[k] = grid_of(r.spec);
     }
     e = ensure_binary64(s);  // lambda and the reverse sweeps use binary64
     if (e != cudaSuccess) return fail_cuda(e, "forward");
     // 2. lambda = H phi, E = Re<phi|lambda>
     bool tiled = false;
-    e = apply_hamiltonian_tiled<T>(s, bufs.lam, H, tiled);
-    if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, bufs.lam, make_groups(H));
+    e = apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
+    if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, sc.lam, make_groups(H));
     if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
-    e = inner_re<T>(s, s.state, bufs.lam, energy);
+    e = inner_re_async<T>(s, s.state, sc.lam);
     if (e != cudaSuccess) return fail_cuda(e, "energy");
     // 3. reverse, segment by segment
-    e = cudaMemsetAsync(bufs.grads, 0, std::max<size_t>(M, 1) * sizeof(double), s.stream);
+    e = cudaMemsetAsync(sc.grads, 0, std::max<size_t>(M, 1) * sizeof(double), s.stream);
     if (e != cudaSuccess) return fail_cuda(e, "gradient buffer");
     for (size_t seg = S; seg-- > 0;) {
-        e = adjoint_segment<P, K, R>(s, bufs, fwd, angles, gtype, b[seg], b[seg + 1], num_sms);
+        const size_t from = seg_first[seg + 1], to = seg > 0 ? seg_first[seg] : sweeps.size();
+        e = run_segment<P, K, R>(s, sc, sweeps, grid, from, to);
         if (e != cudaSuccess) return fail_cuda(e, "reverse sweep");
         if (seg > 0) {
-            e = cudaMemcpyAsync(s.state, bufs.ckpt[seg - 1], sb, cudaMemcpyDeviceToDevice, s.stream);
+            e = cudaMemcpyAsync(s.state, sc.ckpt[seg - 1], sb, cudaMemcpyDeviceToDevice, s.stream);
             if (e != cudaSuccess) return fail_cuda(e, "checkpoint reload");
         }
     }
     grad_per_gate.assign(M, 0.0);
     if (M) {
-        e = copy_async(grad_per_gate.data(), bufs.grads, M * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+        e = copy_async(grad_per_gate.data(), sc.grads, M * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
         if (e != cudaSuccess) return fail_cuda(e, "gradient read-back");
     }
     // leave the handle in |0...0>
     e = init_state(s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) return fail_cuda(e, "finish");
-    bufs.release();
+    *energy = s.h_result[0];
+    // lambda and the checkpoints stay for the next call while they are small
+    // against the device (a sixteenth of its memory); larger ones go now
+    if (sb * (1 + sc.ckpt.size()) > total_b / 16) sc.release_states();
     return KBWG_OK;
 }
 

@@ -292,6 +292,7 @@ int32_t kbwg_free(kbwg_sim *s) {
     s->tmp5.release();
     s->prof.release();
     release_graphs(*s);
+    release_adjoint(*s);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return KBWG_OK;

@@ -77,6 +77,7 @@ struct Sim {
 
     Profiler prof;
     void *graphs = nullptr;  // replay cache of planned sweeps (sweep.cu)
+    void *adj = nullptr;     // adjoint gradient scratch kept between calls (adjoint.cu)
 
     // execution settings of the fused sweeps (0 = built-in default): tile
     // geometry 2^tile_k amplitudes, at most fusion_depth gates per sweep
@@ -104,6 +105,8 @@ cudaError_t ensure_binary64(Sim &s);
 cudaError_t init_state(Sim &s);
 // Free the replay cache of planned sweeps.
 void release_graphs(Sim &s);
+// Free the adjoint gradient's scratch.
+void release_adjoint(Sim &s);
 
 // Build the descriptor of one trait gate: constants computed in the state
 // precision exactly as kbw Dense<F> does (src/dense.rs:211-334).
@@ -118,8 +121,10 @@ cudaError_t run_fused(Sim &s, const GateDesc *gates, size_t count);
 // Specialised kernels (entry point `entry`) for complete sources, following
 // the handle's JIT mode: always: compiled now; auto: from the second request
 // of the same sources on, compiled in the background, loaded once done (null
-// entries until then); off: none.
-std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry);
+// entries until then); off: none.  *final (if given): the answer will not
+// change for these sources (compiled, loaded or failed).
+std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry,
+                                              bool *final = nullptr);
 
 // Wait for the handle's background compilations of specialised kernels;
 // true if any was still to be used (a later flush of its structure loads it).

@@ -210,7 +210,7 @@ struct GraphCache {
 // its forward and its reverse sweeps)
 constexpr size_t kJobEntries = 128;
 constexpr size_t kSeenEntries = 256;
-constexpr size_t kGraphCacheEntries = 8;
+constexpr size_t kGraphCacheEntries = 64;  // (an adjoint's forward pass flushes one structure per segment)
 
 static void free_entry(SweepGraph &g) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -630,8 +630,10 @@ static std::vector<GateDesc> ff_rewrite(const GateDesc *gates, size_t count) {
     return out;
 }
 
-std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry) {
+std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::string> &srcs, const char *entry,
+                                              bool *final) {
     std::vector<const void *> out(srcs.size(), nullptr);
+    if (final) *final = false;
     if (s.jit_mode == KBWG_JIT_OFF || srcs.empty()) return out;
     if (s.jit_mode == KBWG_JIT_AUTO && s.n < jit_min_qubits()) return out;
     if (s.jit_mode == KBWG_JIT_AUTO) {
@@ -665,6 +667,7 @@ std::vector<const void *> specialised_kernels(Sim &s, const std::vector<std::str
         job->used = true;
     }
     for (size_t i = 0; i < srcs.size(); i++) out[i] = jit_kernel(srcs[i], entry);
+    if (final) *final = true;
     return out;
 }
 

@@ -60,6 +60,25 @@ def test_adjoint_checkpoints_do_not_change_result():
     assert abs(e0 - e1) < 1e-13 and np.max(np.abs(g0 - g1)) < 1e-12
 
 
+@pytest.mark.parametrize("prec,fast", [("c64", False), ("c128", True)])
+def test_adjoint_repeated_calls_reuse_scratch(prec, fast):
+    # the handle keeps lambda, the checkpoints and the reverse programs
+    # between calls: repeated, shorter, longer and differently checkpointed
+    # calls give exactly the results of a fresh handle
+    n = 14
+    ham = C.tfim_ring(n)
+    sim = DenseGB300(n, prec, fast_c128=fast)
+    for L, seed, ck in ((3, 1, 16), (1, 2, 16), (5, 3, 2), (3, 1, 16), (2, 4, 0), (3, 1, 16)):
+        params = C.hea_params(n, L, seed)
+        circ, pidx = C.hea(n, L, params), C.hea_param_index(n, L)
+        e, g = sim.adjoint_gradient(circ, pidx, len(params), ham, max_checkpoints=ck)
+        fresh = DenseGB300(n, prec, fast_c128=fast)
+        e2, g2 = fresh.adjoint_gradient(circ, pidx, len(params), ham, max_checkpoints=ck)
+        fresh.close()
+        assert e == e2 and np.array_equal(g, g2), (L, seed, ck)
+    sim.close()
+
+
 def test_adjoint_controlled_phase_shared_params_vs_finite_differences():
     """Controlled rotations, phase gates and a parameter used by two gates:
     compared with central differences (h = 1e-6) of the oracle energy."""
