@@ -40,6 +40,7 @@ namespace kbwg {
 template <class P> struct AdjPolicyName;
 template <> struct AdjPolicyName<FastP> { static constexpr const char *s = "kbwg::FastP"; };
 template <> struct AdjPolicyName<FF2B> { static constexpr const char *s = "kbwg::FF2B"; };
+template <> struct AdjPolicyName<FF2> { static constexpr const char *s = "kbwg::FF2"; };
 template <> struct AdjPolicyName<Fast<double>> { static constexpr const char *s = "kbwg::Fast<double>"; };
 
 // ---- lambda = H phi ------------------------------------------------------------------
@@ -170,6 +171,145 @@ __global__ void __launch_bounds__(256) k_apply_tile(const cx<T> *__restrict__ ph
             lam[gidx] = cx<T>{ar, ai};
         }
         __syncthreads();
+    }
+}
+
+// ---- the same on float-float resident states (complex128 fast path) ----------
+// Amplitudes are ff2::v2 {h = (re.hi, im.hi), l = (re.lo, im.lo)}.  A pass's
+// strings come in runs of one coefficient: Z-type strings with a real
+// factor (no flip) count their signs in an integer and scale the amplitude
+// once per run; real-factor strings with flips add the signed partner
+// amplitudes and scale the sum once per run; complex factors multiply each.
+struct ApplyTileTermFF {
+    uint32_t xl, zl;  // flip and phase masks on local bits
+    uint64_t zo;      // phase mask on qubits outside the tile
+    float rh, rl, ih, il;  // c_k * i^{ny_k} as float-float (re, im)
+    uint32_t cat;     // 0: real, no flip; 1: real with flips; 2: complex
+    uint32_t last;    // 1: the last string of its run
+};
+struct ApplyTilePassFF {
+    uint32_t K, l, m, nterms, init;
+    uint8_t hq[16];
+    ApplyTileTermFF t[kMaxTerms];
+};
+
+__global__ void __launch_bounds__(256) k_apply_tile_ff(const ff2::v2 *__restrict__ phi, ff2::v2 *__restrict__ lam,
+                                                       uint32_t n, const __grid_constant__ ApplyTilePassFF p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ff2::v2 *tile = reinterpret_cast<ff2::v2 *>(smem_raw);
+    const uint32_t K = p.K, l = p.l, m = p.m;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(smem_raw + (sizeof(ff2::v2) << K));
+    for (uint32_t c = threadIdx.x; c < (1u << m); c += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
+        chunk_off[c] = off;
+    }
+    const uint64_t tiles = 1ull << (n - K);
+    const uint32_t lowmask = (1u << l) - 1u;
+    const ff2::v2 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    __syncthreads();
+    for (uint64_t tau = blockIdx.x; tau < tiles; tau += gridDim.x) {
+        uint64_t base = tau << l;
+        for (uint32_t j = 0; j < m; j++) {
+            const uint64_t low = (1ull << p.hq[j]) - 1;
+            base = ((base & ~low) << 1) | (base & low);
+        }
+        for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x)
+            tile[u] = phi[base + chunk_off[u >> l] + (u & lowmask)];
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < (1u << K); u += blockDim.x) {
+            const ff2::v2 self = tile[u];
+            ff2::v2 acc = zero, run = zero;
+            int cnt = 0;
+            for (uint32_t k = 0; k < p.nterms; k++) {  // (branches depend on the term only: uniform)
+                const ApplyTileTermFF &t = p.t[k];
+                const uint32_t src = u ^ t.xl;
+                const bool neg = ((__popc(src & t.zl) + __popcll(base & t.zo)) & 1) != 0;
+                if (t.cat == 0u) {
+                    cnt += neg ? -1 : 1;
+                    if (t.last) {
+                        const ff::f2 w = ff::mul(ff::f2{t.rh, t.rl}, ff::f2{(float)cnt, 0.f});
+                        acc = ff2::add(acc, ff2::mul(self, ff2::konst(w)));
+                        cnt = 0;
+                    }
+                } else if (t.cat == 1u) {
+                    const ff2::v2 a = tile[src];
+                    run = neg ? ff2::sub(run, a) : ff2::add(run, a);
+                    if (t.last) {
+                        acc = ff2::add(acc, ff2::mul(run, ff2::konst(ff::f2{t.rh, t.rl})));
+                        run = zero;
+                    }
+                } else {
+                    const ff2::v2 a = tile[src];
+                    const ff::f2 cr{t.rh, t.rl}, ci{t.ih, t.il};
+                    // (cr re - ci im, cr im + ci re)
+                    const ff2::v2 prod = ff2::dot2(ff2::konst(cr), a, ff2::konst(ff::neg(ci), ci), ff2::swap(a));
+                    acc = neg ? ff2::sub(acc, prod) : ff2::add(acc, prod);
+                }
+            }
+            const uint64_t gidx = base + chunk_off[u >> l] + (u & lowmask);
+            if (!p.init) acc = ff2::add(acc, lam[gidx]);
+            lam[gidx] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// One group of strings with a common flip mask (strings too wide for a
+// tile), float-float: lambda_s (+)= sum_k c_k i^{ny_k} (-1)^{|(s^x) & z_k|} phi_{s^x}.
+__global__ void __launch_bounds__(256) k_apply_group_ff(const ff2::v2 *__restrict__ phi, ff2::v2 *__restrict__ lam,
+                                                        uint64_t ns, ApplyGroup g) {
+    __shared__ float rh[kMaxTerms], rl[kMaxTerms], ih[kMaxTerms], il[kMaxTerms];
+    if (threadIdx.x < kMaxTerms) {
+        const ff::f2 r = ff::split_constant(g.cre[threadIdx.x]), i = ff::split_constant(g.cim[threadIdx.x]);
+        rh[threadIdx.x] = r.h;
+        rl[threadIdx.x] = r.l;
+        ih[threadIdx.x] = i.h;
+        il[threadIdx.x] = i.l;
+    }
+    __syncthreads();
+    const ff2::v2 zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        const uint64_t src = s ^ g.x;
+        const ff2::v2 a = phi[src];
+        ff2::v2 acc = zero;
+        for (uint32_t k = 0; k < g.nterms; k++) {
+            const bool neg = (__popcll(src & g.z[k]) & 1) != 0;
+            const ff::f2 cr{rh[k], rl[k]}, ci{ih[k], il[k]};
+            const ff2::v2 prod = ff2::dot2(ff2::konst(cr), a, ff2::konst(ff::neg(ci), ci), ff2::swap(a));
+            acc = neg ? ff2::sub(acc, prod) : ff2::add(acc, prod);
+        }
+        if (!g.init) acc = ff2::add(acc, lam[s]);
+        lam[s] = acc;
+    }
+}
+
+// Re<a|b> of float-float states: per-thread float-float sums, then FP64.
+__global__ void __launch_bounds__(256) k_inner_re_ff(const ff2::v2 *__restrict__ a, const ff2::v2 *__restrict__ b,
+                                                     uint64_t ns, double *partials, unsigned *ticket, double *result) {
+    ff::f2 t{0.f, 0.f};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        const ff2::v2 x = a[s], y = b[s];
+        t = ff::add(t, ff::dot2(ff::f2{x.h.x, x.l.x}, ff::f2{y.h.x, y.l.x}, ff::f2{x.h.y, x.l.y}, ff::f2{y.h.y, y.l.y}));
+    }
+    double acc = (double)t.h + (double)t.l;
+    __shared__ double sh[8];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += sh[w];
+        partials[blockIdx.x] = tot;
+        __threadfence();
+        if (atomicAdd(ticket, 1u) == gridDim.x - 1) {
+            double all = 0.0;
+            for (unsigned b2 = 0; b2 < gridDim.x; b2++) all += partials[b2];
+            result[0] = all;
+            *ticket = 0;
+        }
     }
 }
 
@@ -653,6 +793,99 @@ static cudaError_t apply_hamiltonian(Sim &s, void *lam, const std::vector<ApplyG
     return cudaSuccess;
 }
 
+// The same passes on float-float resident states: each pass's strings are
+// ordered into runs of one coefficient (Z-type real, real with flips,
+// complex), the form k_apply_tile_ff sums.
+static cudaError_t apply_hamiltonian_tiled_ff(Sim &s, void *lam, const std::vector<PauliString> &H, bool &done) {
+    done = false;
+    const int K = kApplyTileBits;
+    if (s.n < (uint32_t)K + 1 || H.empty()) return cudaSuccess;
+    std::vector<uint64_t> xm;
+    for (const PauliString &t : H) xm.push_back(t.x);
+    std::vector<size_t> wide;
+    const std::vector<PauliPass> passes = plan_pauli_passes(s.n, K, xm, kMaxTerms, wide);
+    if (!wide.empty()) return cudaSuccess;
+    const size_t smem = (sizeof(ff2::v2) << K) + (sizeof(uint64_t) << (K - kLaneBits));
+    {
+        const cudaError_t e = ensure_smem_limit((const void *)k_apply_tile_ff, smem);
+        if (e != cudaSuccess) return e;
+    }
+    const uint64_t tiles = 1ull << (s.n - K);
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, 152ull * 8);
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const PauliPass &pp = passes[pi];
+        ApplyTilePassFF a;
+        memset(&a, 0, sizeof a);
+        a.K = (uint32_t)K;
+        a.l = pp.l;
+        a.m = pp.m;
+        a.init = pi == 0 ? 1u : 0u;
+        memcpy(a.hq, pp.hq, sizeof a.hq);
+        struct Item {
+            ApplyTileTermFF t;
+            double cre, cim;
+        };
+        std::vector<Item> items;
+        for (size_t j = 0; j < pp.members.size(); j++) {
+            const PauliString &ps = H[pp.members[j]];
+            Item it;
+            memset(&it, 0, sizeof it);
+            it.t.xl = pp.local(ps.x);
+            it.t.zl = pp.local(ps.z & pp.tile_mask);
+            it.t.zo = ps.z & ~pp.tile_mask;
+            const int q = ps.ny & 3;  // i^ny
+            it.cre = (q == 0) ? ps.coef : (q == 2 ? -ps.coef : 0.0);
+            it.cim = (q == 1) ? ps.coef : (q == 3 ? -ps.coef : 0.0);
+            it.t.cat = it.cim != 0.0 ? 2u : (it.t.xl == 0u ? 0u : 1u);
+            const ff::f2 r = ff::split_constant(it.cre), i = ff::split_constant(it.cim);
+            it.t.rh = r.h;
+            it.t.rl = r.l;
+            it.t.ih = i.h;
+            it.t.il = i.l;
+            items.push_back(it);
+        }
+        std::stable_sort(items.begin(), items.end(), [](const Item &x, const Item &y) {
+            if (x.t.cat != y.t.cat) return x.t.cat < y.t.cat;
+            if (x.cre != y.cre) return x.cre < y.cre;
+            return x.cim < y.cim;
+        });
+        for (size_t j = 0; j < items.size(); j++) {
+            const bool end = j + 1 == items.size() || items[j + 1].t.cat != items[j].t.cat ||
+                             items[j + 1].cre != items[j].cre || items[j + 1].cim != items[j].cim;
+            items[j].t.last = end ? 1u : 0u;
+            a.t[j] = items[j].t;
+        }
+        a.nterms = (uint32_t)items.size();
+        k_apply_tile_ff<<<grid, 256, smem, s.stream>>>((const ff2::v2 *)s.state, (ff2::v2 *)lam, s.n, a);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    done = true;
+    return cudaSuccess;
+}
+
+static cudaError_t apply_hamiltonian_ff(Sim &s, void *lam, const std::vector<ApplyGroup> &groups) {
+    uint64_t g = (s.ns + 255) / 256;
+    if (g > 152 * 8) g = 152 * 8;
+    for (const ApplyGroup &ag : groups) {
+        k_apply_group_ff<<<(unsigned)g, 256, 0, s.stream>>>((const ff2::v2 *)s.state, (ff2::v2 *)lam, s.ns, ag);
+        count_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+static cudaError_t inner_re_ff_async(Sim &s, const void *a, const void *b) {
+    k_inner_re_ff<<<kReduceBlocks, 256, 0, s.stream>>>((const ff2::v2 *)a, (const ff2::v2 *)b, s.ns, s.rs.partials,
+                                                        s.rs.ticket, s.rs.result);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return copy_async(s.h_result, s.rs.result, sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+}
+
 // Re<a|b> into the handle's pinned result slot; readable after the stream's
 // next synchronisation.
 template <class T>
@@ -701,6 +934,9 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
                            const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
                            std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
     using AK = AdjKernel<P, K, R>;
+    // float-float resident: the forward state, the checkpoints, lambda and
+    // the reverse sweeps all keep the forward sweeps' float-float form
+    constexpr bool kFF = std::is_same<P, FF2>::value;
     if (!s.adj) s.adj = new AdjScratch();
     AdjScratch &sc = *(AdjScratch *)s.adj;
     auto fail_cuda = [&](cudaError_t e, const char *what) {
@@ -757,10 +993,16 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         e = flush_queue(s);
         if (e != cudaSuccess) return fail_cuda(e, "forward");
         if (seg + 1 < S) {
-            // checkpoints are binary64 (the reverse sweeps read that form); a
-            // float-float forward state stays float-float and is exported
-            e = s.ff_resident ? launch_ff_export(s.state, sc.ckpt[seg], s.n, s.stream)
-                              : cudaMemcpyAsync(sc.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
+            // checkpoints take the reverse sweeps' form: float-float copies,
+            // or binary64 (a float-float forward state is exported)
+            if (kFF && !s.ff_resident) {
+                e = launch_ff_convert(s.state, s.n, true, s.stream);
+                if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
+                s.ff_resident = true;
+            }
+            e = (!kFF && s.ff_resident)
+                    ? launch_ff_export(s.state, sc.ckpt[seg], s.n, s.stream)
+                    : cudaMemcpyAsync(sc.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
             if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
         }
     }
@@ -817,14 +1059,26 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         r.a.partials = sc.partials;
         grid[k] = grid_of(r.spec);
     }
-    e = ensure_binary64(s);  // lambda and the reverse sweeps use binary64
+    if (kFF) {
+        if (!s.ff_resident) {
+            e = launch_ff_convert(s.state, s.n, true, s.stream);
+            s.ff_resident = true;
+        }
+    } else {
+        e = ensure_binary64(s);  // lambda and the reverse sweeps use binary64
+    }
     if (e != cudaSuccess) return fail_cuda(e, "forward");
     // 2. lambda = H phi, E = Re<phi|lambda>
     bool tiled = false;
-    e = apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
-    if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, sc.lam, make_groups(H));
+    if (kFF) {
+        e = apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled);
+        if (e == cudaSuccess && !tiled) e = apply_hamiltonian_ff(s, sc.lam, make_groups(H));
+    } else {
+        e = apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
+        if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, sc.lam, make_groups(H));
+    }
     if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
-    e = inner_re_async<T>(s, s.state, sc.lam);
+    e = kFF ? inner_re_ff_async(s, s.state, sc.lam) : inner_re_async<T>(s, s.state, sc.lam);
     if (e != cudaSuccess) return fail_cuda(e, "energy");
     // 3. reverse, segment by segment
     e = cudaMemsetAsync(sc.grads, 0, std::max<size_t>(M, 1) * sizeof(double), s.stream);
@@ -889,6 +1143,8 @@ size_t jit_check_adjoint(const Sim &s, const std::vector<GateDesc> &fwd, const s
         return check_adjoint_p<FastP, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, gtype, sweeps);
     }
     if (s.n < (uint32_t)AdjCfg<double>::K) return 0;
+    if (ff_capable(s))
+        return check_adjoint_p<FF2, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, gtype, sweeps);
     if (s.flags & KBWG_FLAG_FAST_C128)
         return check_adjoint_p<FF2B, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, gtype, sweeps);
     return check_adjoint_p<Fast<double>, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, gtype, sweeps);
@@ -908,6 +1164,9 @@ int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::ve
     if (s.prec == 0)
         return adjoint_run<FastP, float, AdjCfg<float>::K, AdjCfg<float>::R>(s, fwd, angles, gtype, H, energy,
                                                                                  grad_per_gate, max_ckpt);
+    if (ff_capable(s))  // the forward state stays float-float
+        return adjoint_run<FF2, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
+                                                                            grad_per_gate, max_ckpt);
     if (s.flags & KBWG_FLAG_FAST_C128)
         return adjoint_run<FF2B, double, AdjCfg<double>::K, AdjCfg<double>::R>(s, fwd, angles, gtype, H, energy,
                                                                              grad_per_gate, max_ckpt);

@@ -140,6 +140,10 @@ struct Grad<FF2B> {
     static __device__ __forceinline__ double wvalue(Wacc w) { return G1::wvalue(w); }
 };
 
+// Float-float resident states (the forward sweeps' form): the same terms.
+template <>
+struct Grad<FF2> : Grad<FF2B> {};
+
 template <class P, int R, int B>
 __device__ __forceinline__ typename Grad<P>::Acc grad_pairs(int gt, const typename P::Amp (&ph)[1 << R],
                                                            const typename P::Amp (&la)[1 << R], uint32_t creg) {

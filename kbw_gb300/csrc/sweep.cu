@@ -684,7 +684,9 @@ bool wait_specialised(Sim &s) {
 }
 
 bool ff_capable(const Sim &s) {
-    return s.prec && (s.flags & KBWG_FLAG_FAST_C128) && s.n >= (uint32_t)TileCfgFF::K;
+    // (one kernel per gate, KBWG_FLAG_NO_FUSION, runs on binary64)
+    return s.prec && (s.flags & KBWG_FLAG_FAST_C128) && !(s.flags & KBWG_FLAG_NO_FUSION) &&
+           s.n >= (uint32_t)TileCfgFF::K;
 }
 
 cudaError_t ensure_binary64(Sim &s) {

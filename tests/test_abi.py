@@ -212,7 +212,8 @@ def test_planner_long_lists_and_stage_limit(lib, prec):
     assert rel_err(o.state(), ref.state()) < tol
 
 
-@pytest.mark.parametrize("prec,flags", [(N.C64, 0), (N.C128, N.FLAG_FAST_C128), (N.C128, 0)])
+@pytest.mark.parametrize("prec,flags", [(N.C64, 0), (N.C128, N.FLAG_FAST_C128), (N.C128, 0),
+                                        (N.C128, N.FLAG_FAST_C128 | N.FLAG_NO_FUSION)])
 def test_specialised_adjoint_kernels_compile(lib, prec, flags):
     """The specialised reverse sweeps of the adjoint gradient compile for
     every arithmetic (host only): a hardware-efficient ansatz and a random

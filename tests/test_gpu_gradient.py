@@ -79,6 +79,35 @@ def test_adjoint_repeated_calls_reuse_scratch(prec, fast):
     sim.close()
 
 
+@pytest.mark.parametrize("fusion,wide", [(True, False), (True, True), (False, False)])
+def test_adjoint_float_float_forms_vs_binary64(fusion, wide):
+    # float-float complex128: with fused sweeps the whole gradient stays in
+    # the float-float form (checkpoints, lambda, reverse sweeps); with one
+    # kernel per gate the forward pass is binary64 and the reverse sweeps
+    # split it on load.  Both agree with the binary64 adjoint within 1e-12,
+    # with lambda in tiled passes or (a wide string) by flip-mask groups.
+    n, L = 13, 3
+    params = C.hea_params(n, L, 8)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    extra = C.random_circuit(n, 40, 21, max_controls=1, kinds=[C.RX, C.RY, C.RZ, C.P, C.H, C.Y])
+    k = len(params)
+    for g in extra:
+        circ.append(g)
+        pidx.append(k if g[0] in C.PARAMETRIC else -1)
+        k += 1 if g[0] in C.PARAMETRIC else 0
+    ham = C.tfim_ring(n) + [(1.5, [(C.PAULI_Y, 2), (C.PAULI_Y, 7)]), (-0.25, [(C.PAULI_Y, 4)]),
+                            (0.5, [(C.PAULI_X, 0), (C.PAULI_Z, 12)])]
+    if wide:  # a string flipping more qubits than a tile holds: lambda by flip-mask groups
+        ham.append((0.3, [(C.PAULI_X, q) for q in range(n)]))
+    ref = DenseGB300(n, "c128")
+    e0, g0 = ref.adjoint_gradient(circ, pidx, k, ham, max_checkpoints=3)
+    sim = DenseGB300(n, "c128", fast_c128=True, fusion=fusion)
+    e1, g1 = sim.adjoint_gradient(circ, pidx, k, ham, max_checkpoints=3)
+    assert abs(e1 - e0) < 1e-12
+    assert np.max(np.abs(g1 - g0)) < 1e-12, np.max(np.abs(g1 - g0))
+
+
 def test_adjoint_controlled_phase_shared_params_vs_finite_differences():
     """Controlled rotations, phase gates and a parameter used by two gates:
     compared with central differences (h = 1e-6) of the oracle energy."""
