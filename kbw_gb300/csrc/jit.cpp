@@ -277,29 +277,52 @@ std::string side_of(const TileGate &t) {
     return buf;
 }
 
-// Statement applying gate t (constants in `k`) to the registers `v`; the
-// control outside the tile is left to the caller.
-std::string gate_stmt(const TileGate &t, const char *v, const char *k) {
+// Condition of a gate's controls outside the tile ("" if none).
+std::string outer_cond(const TileGate &t, bool wide) {
+    if (!t.co) return "";
+    char buf[96];
+    if (wide)
+        snprintf(buf, sizeof buf, "((base & 0x%llxull) == 0x%llxull)", (unsigned long long)t.co,
+                 (unsigned long long)t.co);
+    else
+        snprintf(buf, sizeof buf, "((base & 0x%xu) == 0x%xu)", (uint32_t)t.co, (uint32_t)t.co);
+    return buf;
+}
+
+// Statement applying gate t (constants in `k`) to the registers `v`, with
+// its controls on lane/warp bits and the condition `outer` of its controls
+// outside the tile ("": none, or left to the caller).  Lane-bit gates,
+// register-bit X and diagonal gates take the condition as a per-register
+// select; other register-bit gates run under a branch.
+std::string gate_stmt(const TileGate &t, const char *v, const char *k, const std::string &outer) {
     char buf[512];
     const char *cls = kClassName[t.cls];
     const int q = (t.cls == TG_PI) ? (int)t.c[0] : 0;
+    std::string cond;
+    if (t.fneed) cond = fok_of(t);
+    if (!outer.empty()) cond = cond.empty() ? outer : cond + " && " + outer;
+    const std::string c = cond.empty() ? "true" : cond;
     if (t.op < OP_REG) {
         snprintf(buf, sizeof buf, "jit::lane<P, R, %d, %s, 0x%xu, %d>(%s, %s, %s, F);", (int)t.tb, cls, t.creg,
-                 (int)t.sub, v, k, fok_of(t).c_str());
+                 (int)t.sub, v, k, c.c_str());
         return buf;
     }
-    if (t.op < OP_DREG)
+    if (t.op < OP_DREG) {
+        if (!cond.empty() && t.cls == TG_X) {
+            snprintf(buf, sizeof buf, "jit::cswap<P, R, %d, 0x%xu>(%s, %s);", (int)t.rb, (unsigned)t.jm, v, c.c_str());
+            return buf;
+        }
         snprintf(buf, sizeof buf, "jit::reg<P, R, %d, %s, 0x%xu, %d>(%s, %s);", (int)t.rb, cls, (unsigned)t.jm,
                  (int)t.sub, v, k);
-    else if (t.op < OP_DFIX)
-        snprintf(buf, sizeof buf, "jit::dreg<P, R, %d, %s, 0x%xu, %d>(%s, %s);", (int)t.rb, cls, (unsigned)t.jm, q, v,
-                 k);
+        return cond.empty() ? std::string(buf) : "if (" + cond + ") { " + buf + " }";
+    }
+    if (t.op < OP_DFIX)
+        snprintf(buf, sizeof buf, "jit::dreg<P, R, %d, %s, 0x%xu, %d>(%s, %s, %s);", (int)t.rb, cls, (unsigned)t.jm, q,
+                 v, k, c.c_str());
     else
-        snprintf(buf, sizeof buf, "jit::dfix<P, R, %s, 0x%xu, %d>(%s, %s, %s);", cls, (unsigned)t.jm, q, v, k,
-                 side_of(t).c_str());
-    std::string st = buf;
-    if (t.fneed) st = "if (" + fok_of(t) + ") { " + st + " }";
-    return st;
+        snprintf(buf, sizeof buf, "jit::dfix<P, R, %s, 0x%xu, %d>(%s, %s, %s, %s);", cls, (unsigned)t.jm, q, v, k,
+                 side_of(t).c_str(), c.c_str());
+    return buf;
 }
 
 // Guard of a gate with controls outside the tile (uniform over the tile).
@@ -347,7 +370,7 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
         const size_t g1 = sw.stage_end[st];
         for (size_t i = g0; i < g1; i++) {
             const TileGate &t = sw.gates[i];
-            s += "    " + outer_guard(t, gate_stmt(t, "v", constants_of(t, i).c_str()), geo.wide) + "\n";
+            s += "    " + gate_stmt(t, "v", constants_of(t, i).c_str(), outer_cond(t, geo.wide)) + "\n";
         }
         g0 = g1;
     }
@@ -421,7 +444,7 @@ std::string jit_adjoint_source(const JitGeometry &geo, const PlannedSweep &sw, c
             const std::string k = constants_of(t, i);
             if (k != "kz") body += "const typename P::K4 k = " + k + "; ";
             const char *kv = (k != "kz") ? "k" : "kz";
-            body += gate_stmt(t, "vp", kv) + " " + gate_stmt(t, "vl", kv);
+            body += gate_stmt(t, "vp", kv, "") + " " + gate_stmt(t, "vl", kv, "");
             s += "    " + outer_guard(t, "{ " + body + " }", true) + "\n";
         }
         g0 = g1;

@@ -46,6 +46,28 @@ __device__ __forceinline__ void reg(typename P::Amp (&v)[1 << R], const typename
     }
 }
 
+template <class A>
+__device__ __forceinline__ A sel(bool c, const A &x, const A &y) {
+    return c ? x : y;
+}
+
+// Register-bit X when `c` holds (controls on lane/warp bits or outside the
+// tile): per-pair selects rather than a branch around the block, so both
+// sides keep one register assignment (a branch made the compiler carry two
+// copies of the registers and spill).
+template <class P, int R, int B, uint32_t JM>
+__device__ __forceinline__ void cswap(typename P::Amp (&v)[1 << R], bool c) {
+#pragma unroll
+    for (int jj = 0; jj < (1 << (R - 1)); jj++) {
+        const int j0 = ((jj >> B) << (B + 1)) | (jj & ((1 << B) - 1));
+        const int j1 = j0 | (1 << B);
+        if (((JM >> j0) & 1u) == 0u) continue;
+        const typename P::Amp a = v[j0], b = v[j1];
+        v[j0] = sel(c, b, a);
+        v[j1] = sel(c, a, b);
+    }
+}
+
 // Non-diagonal gate whose target is lane bit TB: the partner amplitude comes
 // from lane ^ (1 << TB).  Registers whose register-bit controls fail (CREG)
 // take no part, in any lane; `fok` (controls on lane/warp bits) selects per
@@ -72,42 +94,51 @@ __device__ __forceinline__ void lane(typename P::Amp (&v)[1 << R], const typenam
     }
 }
 
-// Diagonal gate whose target is register bit B (Q: the power of i of a PI gate).
+// Diagonal gate whose target is register bit B (Q: the power of i of a PI
+// gate), applied where `c` holds (its controls off the registers).
 template <class P, int R, int B, int CLS, uint32_t JM, int Q>
-__device__ __forceinline__ void dreg(typename P::Amp (&v)[1 << R], const typename P::K4 &k) {
+__device__ __forceinline__ void dreg(typename P::Amp (&v)[1 << R], const typename P::K4 &k, bool c = true) {
 #pragma unroll
     for (int j = 0; j < (1 << R); j++) {
         if (((JM >> j) & 1u) == 0u) continue;
         const bool hi = ((j >> B) & 1) != 0;
         if constexpr (CLS == TG_Z) {
-            if (hi) v[j] = P::neg(v[j]);
+            if (hi) v[j] = sel(c, P::neg(v[j]), v[j]);
         } else if constexpr (CLS == TG_P) {
-            if (hi) v[j] = P::cmul(v[j], k.c0, k.c1);
+            if (hi) v[j] = sel(c, P::cmul(v[j], k.c0, k.c1), v[j]);
         } else if constexpr (CLS == TG_RZ) {
-            v[j] = hi ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1);
+            v[j] = sel(c, hi ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1), v[j]);
         } else {  // TG_PI
-            if (hi) v[j] = P::pi_mul(v[j], Q);
+            if (hi) v[j] = sel(c, P::pi_mul(v[j], Q), v[j]);
         }
     }
 }
 
 // Diagonal gate whose target side `one` is the same for all of a thread's
-// registers (a lane or warp bit, a qubit outside the tile; SCALE: always).
+// registers (a lane or warp bit, a qubit outside the tile; SCALE: always),
+// applied where `c` holds.  Per-register selects (RZ: of the constants)
+// rather than a branch around the block; each amplitude gets the
+// arithmetic the branch would give it.
 template <class P, int R, int CLS, uint32_t JM, int Q>
-__device__ __forceinline__ void dfix(typename P::Amp (&v)[1 << R], const typename P::K4 &k, bool one) {
-    if constexpr (CLS != TG_SCALE && CLS != TG_RZ)
-        if (!one) return;
+__device__ __forceinline__ void dfix(typename P::Amp (&v)[1 << R], const typename P::K4 &k, bool one, bool c = true) {
+    if constexpr (CLS == TG_RZ) {
+        const auto cr = one ? k.c2 : k.c0;
+        const auto ci = one ? k.c3 : k.c1;
 #pragma unroll
-    for (int j = 0; j < (1 << R); j++) {
-        if (((JM >> j) & 1u) == 0u) continue;
-        if constexpr (CLS == TG_Z) {
-            v[j] = P::neg(v[j]);
-        } else if constexpr (CLS == TG_PI) {
-            v[j] = P::pi_mul(v[j], Q);
-        } else if constexpr (CLS == TG_RZ) {
-            v[j] = one ? P::cmul(v[j], k.c2, k.c3) : P::cmul(v[j], k.c0, k.c1);
-        } else {  // P (|1> side only, `one` checked above) and SCALE
-            v[j] = P::cmul(v[j], k.c0, k.c1);
+        for (int j = 0; j < (1 << R); j++)
+            if ((JM >> j) & 1u) v[j] = sel(c, P::cmul(v[j], cr, ci), v[j]);
+    } else {
+        const bool on = (CLS == TG_SCALE || one) && c;
+#pragma unroll
+        for (int j = 0; j < (1 << R); j++) {
+            if (((JM >> j) & 1u) == 0u) continue;
+            if constexpr (CLS == TG_Z) {
+                v[j] = sel(on, P::neg(v[j]), v[j]);
+            } else if constexpr (CLS == TG_PI) {
+                v[j] = sel(on, P::pi_mul(v[j], Q), v[j]);
+            } else {  // P (|1> side only) and SCALE
+                v[j] = sel(on, P::cmul(v[j], k.c0, k.c1), v[j]);
+            }
         }
     }
 }
