@@ -77,8 +77,8 @@ enum {
  * Allocates 2^num_qubits amplitudes in |0...0>.  Dense::new stops at 32
  * qubits; DenseGPU and the Block backends have no cap (src/c_api.rs:93-109),
  * and neither has this engine below 40 (KBWG_EQUBITS above): the device's
- * memory decides (KBWG_ENOMEM), one GB300 holding 33 qubits in complex128 or
- * 34 in complex64.  Above 32 qubits gates run in the default tile geometry
+ * memory decides (KBWG_ENOMEM), one GB300 holding 34 qubits in complex128 or
+ * 35 in complex64 (256 GiB).  Above 32 qubits gates run in the default tile geometry
  * with 64-bit state indices; the adjoint gradient stays at 32 qubits. */
 int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_sim **out);
 

@@ -47,7 +47,7 @@ struct Profiler {
 // Largest register: Dense/DenseV2 stop at 32 qubits (src/dense.rs:71-73),
 // DenseGPU and the Block backends have no cap (src/c_api.rs:93-109); here the
 // tile kernels index tiles with 32 bits (2^(n - K) tiles) and the device's
-// memory decides below that (one GB300: 33 qubits complex128 or 34 complex64).
+// memory decides below that (one GB300: 34 qubits complex128 or 35 complex64).
 constexpr uintptr_t kMaxQubits = 40;
 
 struct Sim {

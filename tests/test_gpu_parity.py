@@ -561,10 +561,12 @@ def test_own_generator_is_stdrng_of_kbw_seed(monkeypatch):
     b.close()
 
 
-@pytest.mark.parametrize("n,prec,fast", [(33, "c128", True), (33, "c128", False), (34, "c64", False)])
+@pytest.mark.parametrize("n,prec,fast", [(33, "c128", True), (33, "c128", False), (34, "c64", False),
+                                         (34, "c128", True), (35, "c64", False)])
 def test_registers_above_32_qubits(n, prec, fast):
     """Beyond Dense's 32 qubits (DenseGPU and the Block backends have no cap):
-    128 GiB of amplitudes on one GB300, swept with 64-bit state indices.  A
+    128 and 256 GiB of amplitudes (256 GiB: the largest power of two that
+    fits in one GB300's HBM), swept with 64-bit state indices.  A
     random circuit with controls on the top qubits keeps the norm, its
     inverse returns |0...0>, and a Bell pair between the top and the bottom
     qubit reads out exactly (dump, p1, measurement with injected draws)."""
