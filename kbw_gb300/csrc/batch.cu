@@ -44,11 +44,30 @@ struct BatchSweep {
 struct BatchJob {
     uint32_t n, nsweeps, sweep_off, nterms;
     uint32_t term_off, id, pad;
+    uint32_t pass_off, npasses;  // tiled <H> passes (registers larger than a tile)
 };
 
 struct BatchTerm {
     uint64_t x, z;
     double cr, ci;  // c_k * i^{ny}: the string's share of conj(a_s) a_{s^x} is sign * (cr p.re - ci p.im)
+};
+
+// One tiled <H> pass of a register larger than a tile: tiles of 2^K
+// amplitudes (2^l contiguous ones per chunk, the chunks picked by the m
+// qubits hq) hold both a_s and a_{s^x} for every string of the pass.
+struct BatchPass {
+    uint32_t l, m, term_off, nterms;
+    uint8_t hq[16];
+};
+// A string of a pass: flip and phase masks on the tile's local bits, phase
+// mask on the qubits outside it; `last` closes a run of strings with the
+// same flip mask and coefficient (their signs are counted, the coefficient
+// applied once); `newx`: the first string of a flip mask.
+struct BatchTileTerm {
+    uint32_t xl, zl;
+    uint64_t zo;
+    double cr, ci;
+    uint32_t last, newx;
 };
 
 struct BatchArgs {
@@ -58,6 +77,8 @@ struct BatchArgs {
     const BatchSweep *sweeps;
     const TileGate *prog;
     const BatchTerm *terms;
+    const BatchPass *passes;
+    const BatchTileTerm *tterms;
     double *energies;
     void *slots;
     uint64_t slot_elems;
@@ -96,6 +117,89 @@ __device__ __forceinline__ Mem batch_basis(bool one) {
     m.re = one ? 1 : 0;
     m.im = 0;
     return m;
+}
+
+// <H> of a register larger than a tile, in tiled passes: each tile staged
+// once per pass (TMA), every string of the pass summed from shared memory.
+// (Its own function: the sweep loop keeps its register allocation.)
+template <class P, int K, int R>
+__device__ __noinline__ bool batch_energy_passes(const BatchArgs &a, const BatchJob &job, typename P::Mem *slot,
+                                                 typename P::Mem *tile_mem, uint64_t *chunk_off, uint64_t *bar,
+                                                 uint32_t &phase, double &sum) {
+    using Mem = typename P::Mem;
+    using T = decltype(Mem{}.re);
+    BatchAcc<T> acc;  // (local: the caller's accumulator would live in memory across the call)
+    using BK = BatchKernel<P, K, R>;
+    constexpr int NR = 1 << R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t n = job.n;
+    for (uint32_t pi = 0; pi < job.npasses; pi++) {
+        const BatchPass &bp = a.passes[job.pass_off + pi];
+        const uint32_t l = bp.l, m = bp.m;
+        const uint32_t chunk = 1u << l, nchunks = 1u << m;
+        for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
+            uint64_t off = 0;
+            for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << bp.hq[j];
+            chunk_off[c] = off;
+        }
+        __syncthreads();
+        const uint64_t tiles = 1ull << (n - K);
+        const BatchTileTerm *tt = a.tterms + bp.term_off;
+        for (uint64_t tau = 0; tau < tiles; tau++) {
+            uint64_t base = tau << l;
+            for (uint32_t j = 0; j < m; j++) base = insert_zero_at(base, bp.hq[j]);
+            if (warp == 0) {
+                if (lane == 0) mbar_expect_tx(bar, (uint32_t)BK::kTileBytes);
+                __syncwarp();
+                for (uint32_t c = lane; c < nchunks; c += 32)
+                    tma_load(tile_mem + (size_t)c * chunk, slot + base + chunk_off[c], chunk * (uint32_t)sizeof(Mem),
+                             bar);
+            }
+            if (!tile_wait(bar, phase & 1u, a.err)) return false;
+            phase++;
+            // each thread's NR amplitudes u = tid + i * threads in registers;
+            // strings outer (their fields read once per tile), signs counted
+            // per amplitude, the product formed once per run
+            T ar[NR], ai[NR];
+            int cnt[NR];
+#pragma unroll
+            for (int i = 0; i < NR; i++) {
+                const Mem m2 = tile_mem[threadIdx.x + (uint32_t)i * BK::kThreads];
+                ar[i] = m2.re;
+                ai[i] = m2.im;
+                cnt[i] = 0;
+            }
+            for (uint32_t k = 0; k < bp.nterms; k++) {
+                const BatchTileTerm t = tt[k];
+                const uint32_t op = (uint32_t)__popcll(base & t.zo) & 1u;
+#pragma unroll
+                for (int i = 0; i < NR; i++) {
+                    const uint32_t u = threadIdx.x + (uint32_t)i * BK::kThreads;
+                    cnt[i] += (((uint32_t)__popc((u ^ t.xl) & t.zl) + op) & 1u) ? -1 : 1;
+                }
+                if (t.last) {  // (uniform)
+#pragma unroll
+                    for (int i = 0; i < NR; i++) {
+                        const uint32_t u = threadIdx.x + (uint32_t)i * BK::kThreads;
+                        T pr, pim;  // conj(a_u) a_{u^x}
+                        if (t.xl == 0u) {
+                            pr = ar[i] * ar[i] + ai[i] * ai[i];
+                            pim = (T)0;
+                        } else {
+                            const Mem ax = tile_mem[u ^ t.xl];
+                            pr = ar[i] * ax.re + ai[i] * ax.im;
+                            pim = ar[i] * ax.im - ai[i] * ax.re;
+                        }
+                        acc.add((T)cnt[i] * ((T)t.cr * pr - (T)t.ci * pim));
+                        cnt[i] = 0;
+                    }
+                }
+            }
+            __syncthreads();  // the tile is read no more: the next load may land
+        }
+    }
+    sum = acc.value();
+    return true;
 }
 
 template <class P, int K, int R>
@@ -159,9 +263,26 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
             const uint64_t tiles = in_tile ? 1ull : (1ull << (n - K));
             const uint32_t chunk = 1u << l, nchunks = 1u << m;
             const uint64_t lowmask = chunk - 1;
+            auto tile_base = [&](uint64_t t) {
+                uint64_t b = t << l;
+                for (uint32_t j = 0; j < m; j++) b = insert_zero_at(b, bs.hq[j]);
+                return b;
+            };
+            // the slot's tiles: tile tau + 1's load is issued before tile tau's
+            // stores (the tiles of a sweep are disjoint)
+            auto issue_load = [&](uint64_t t) {
+                if (warp == 0) {
+                    const uint64_t b = tile_base(t);
+                    if (lane == 0) mbar_expect_tx(bar, (uint32_t)BK::kTileBytes);
+                    __syncwarp();
+                    for (uint32_t c = lane; c < nchunks; c += 32)
+                        tma_load(tile_mem + (size_t)c * chunk, slot + b + chunk_off[c], chunk * (uint32_t)sizeof(Mem),
+                                 bar);
+                }
+            };
+            if (!in_tile) issue_load(0);
             for (uint64_t tau = 0; tau < tiles; tau++) {
-                uint64_t base = tau << l;
-                for (uint32_t j = 0; j < m; j++) base = insert_zero_at(base, bs.hq[j]);
+                const uint64_t base = tile_base(tau);
                 int layout = bs.stage_layout[0];
                 int R0 = (layout == LAYOUT_A) ? kLaneBits : (K - R);
                 uint32_t F = (layout == LAYOUT_A) ? FA : FB;
@@ -170,13 +291,6 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
 #pragma unroll
                     for (int j = 0; j < NR; j++) v[j] = tile[F | ((uint32_t)j << R0)];
                 } else {
-                    if (warp == 0) {
-                        if (lane == 0) mbar_expect_tx(bar, (uint32_t)BK::kTileBytes);
-                        __syncwarp();
-                        for (uint32_t c = lane; c < nchunks; c += 32)
-                            tma_load(tile_mem + (size_t)c * chunk, slot + base + chunk_off[c],
-                                     chunk * (uint32_t)sizeof(Mem), bar);
-                    }
                     if (!tile_wait(bar, phase & 1u, a.err)) return;
                     phase++;
 #pragma unroll
@@ -207,6 +321,7 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
                     // the tile buffer is read no more (next tile's load) once all threads pass here
                     fence_proxy_async();
                     __syncthreads();
+                    if (tau + 1 < tiles) issue_load(tau + 1);
 #pragma unroll
                     for (int j = 0; j < NR; j++) {
                         const uint32_t u = F | ((uint32_t)j << R0);
@@ -219,6 +334,9 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
         }
         // ---- <H> ----
         BatchAcc<T> acc;
+        // tiled passes (registers larger than a tile)
+        double tiled = 0.0;
+        if (job.npasses && !batch_energy_passes<P, K, R>(a, job, slot, tile_mem, chunk_off, bar, phase, tiled)) return;
         const uint64_t ns = 1ull << n;
         for (uint32_t t0 = 0; t0 < job.nterms;) {
             const uint64_t x = a.terms[job.term_off + t0].x;
@@ -245,7 +363,7 @@ __global__ void __launch_bounds__(BatchKernel<P, K, R>::kThreads, 2) k_batch_cir
             }
             t0 = t1;
         }
-        double e = acc.value();
+        double e = acc.value() + tiled;
         for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
         if (lane == 0) red[warp] = e;
         __syncthreads();
@@ -265,6 +383,8 @@ struct BatchCircuitIn {
     // the circuit's plan (batch_run)
     std::vector<BatchSweep> sweeps;
     std::vector<TileGate> prog;
+    std::vector<BatchPass> passes;       // tiled <H> passes (n > K); then `terms`
+    std::vector<BatchTileTerm> tterms;   // holds only the strings too wide for a tile
     bool placed = true;
     // validation result
     int32_t status = KBWG_OK;
@@ -324,11 +444,55 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
             ci.sweeps.push_back(b);
         }
         ci.placed = placed == ci.gates.size();
+        if (ci.n > (uint32_t)K && !ci.terms.empty()) {
+            std::vector<uint64_t> xm;
+            for (const BatchTerm &t : ci.terms) xm.push_back(t.x);
+            std::vector<size_t> wide;
+            const std::vector<PauliPass> pp = plan_pauli_passes(ci.n, K, xm, (size_t)-1, wide);
+            for (const PauliPass &ps : pp) {
+                BatchPass b;
+                memset(&b, 0, sizeof b);
+                b.l = ps.l;
+                b.m = ps.m;
+                memcpy(b.hq, ps.hq, sizeof b.hq);
+                b.term_off = (uint32_t)ci.tterms.size();  // within the circuit; rebased below
+                std::vector<BatchTileTerm> ts;
+                for (size_t k : ps.members) {
+                    const BatchTerm &t = ci.terms[k];
+                    BatchTileTerm q;
+                    memset(&q, 0, sizeof q);
+                    q.xl = ps.local(t.x);
+                    q.zl = ps.local(t.z & ps.tile_mask);
+                    q.zo = t.z & ~ps.tile_mask;
+                    q.cr = t.cr;
+                    q.ci = t.ci;
+                    ts.push_back(q);
+                }
+                std::stable_sort(ts.begin(), ts.end(), [](const BatchTileTerm &x, const BatchTileTerm &y) {
+                    if (x.xl != y.xl) return x.xl < y.xl;
+                    if (x.cr != y.cr) return x.cr < y.cr;
+                    return x.ci < y.ci;
+                });
+                for (size_t j = 0; j < ts.size(); j++) {
+                    ts[j].newx = (j == 0 || ts[j - 1].xl != ts[j].xl) ? 1u : 0u;
+                    const bool end = j + 1 == ts.size() || ts[j + 1].xl != ts[j].xl || ts[j + 1].cr != ts[j].cr ||
+                                     ts[j + 1].ci != ts[j].ci;
+                    ts[j].last = end ? 1u : 0u;
+                }
+                b.nterms = (uint32_t)ts.size();
+                ci.tterms.insert(ci.tterms.end(), ts.begin(), ts.end());
+                ci.passes.push_back(b);
+            }
+            std::vector<BatchTerm> rest;  // (wide keeps the flip-mask order)
+            for (size_t k : wide) rest.push_back(ci.terms[k]);
+            ci.terms.swap(rest);
+        }
     });
     // lay the programs out one after another: offsets first, then the copies
     // (in parallel again) into arrays sized once
     std::vector<BatchJob> jobs(circs.size());
-    size_t nsweeps = 0, nprog = 0, nterms = 0;
+    size_t nsweeps = 0, nprog = 0, nterms = 0, npass = 0, ntt = 0;
+    std::vector<uint32_t> tt_off(circs.size());
     uint32_t nmax = 0;
     for (size_t c = 0; c < circs.size(); c++) {
         const BatchCircuitIn &ci = circs[c];
@@ -345,18 +509,25 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
         j.term_off = (uint32_t)nterms;
         j.nterms = (uint32_t)ci.terms.size();
         j.pad = (uint32_t)nprog;  // the circuit's first gate, for the copies below
+        j.pass_off = (uint32_t)npass;
+        j.npasses = (uint32_t)ci.passes.size();
+        tt_off[c] = (uint32_t)ntt;
         nsweeps += ci.sweeps.size();
         nprog += ci.prog.size();
         nterms += ci.terms.size();
+        npass += ci.passes.size();
+        ntt += ci.tterms.size();
         nmax = std::max(nmax, ci.n);
     }
-    if (nprog > UINT32_MAX || nsweeps > UINT32_MAX || nterms > UINT32_MAX) {
+    if (nprog > UINT32_MAX || nsweeps > UINT32_MAX || nterms > UINT32_MAX || ntt > UINT32_MAX) {
         set_error(KBWG_EINVAL, "batch circuits: more than 2^32 planned gates, sweeps or strings");
         return KBWG_EINVAL;
     }
     std::unique_ptr<BatchSweep[]> sweeps(new BatchSweep[std::max<size_t>(nsweeps, 1)]);
     std::unique_ptr<TileGate[]> prog(new TileGate[std::max<size_t>(nprog, 1)]);
     std::unique_ptr<BatchTerm[]> terms(new BatchTerm[std::max<size_t>(nterms, 1)]);
+    std::unique_ptr<BatchPass[]> passes(new BatchPass[std::max<size_t>(npass, 1)]);
+    std::unique_ptr<BatchTileTerm[]> tterms(new BatchTileTerm[std::max<size_t>(ntt, 1)]);
     batch_parallel_for(circs.size(), [&](size_t c) {
         BatchCircuitIn &ci = circs[c];
         BatchJob &j = jobs[c];
@@ -369,6 +540,13 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
         }
         if (!ci.prog.empty()) memcpy(&prog[base], ci.prog.data(), ci.prog.size() * sizeof(TileGate));
         if (!ci.terms.empty()) memcpy(&terms[j.term_off], ci.terms.data(), ci.terms.size() * sizeof(BatchTerm));
+        for (size_t i = 0; i < ci.passes.size(); i++) {
+            BatchPass b = ci.passes[i];
+            b.term_off += tt_off[c];
+            passes[j.pass_off + i] = b;
+        }
+        if (!ci.tterms.empty())
+            memcpy(&tterms[tt_off[c]], ci.tterms.data(), ci.tterms.size() * sizeof(BatchTileTerm));
     });
     // largest first: the persistent CTAs then finish together
     std::stable_sort(jobs.begin(), jobs.end(), [&](const BatchJob &x, const BatchJob &y) {
@@ -390,9 +568,11 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
     const size_t jb = jobs.size() * sizeof(BatchJob), swb = std::max<size_t>(nsweeps, 1) * sizeof(BatchSweep),
                  pb = std::max<size_t>(nprog, 1) * sizeof(TileGate),
                  tb = std::max<size_t>(nterms, 1) * sizeof(BatchTerm), eb = circs.size() * sizeof(double),
+                 pab = std::max<size_t>(npass, 1) * sizeof(BatchPass),
+                 ttb = std::max<size_t>(ntt, 1) * sizeof(BatchTileTerm),
                  sb = (size_t)grid * slot_elems * sizeof(Mem);
-    const size_t o_sw = up(jb), o_p = o_sw + up(swb), o_t = o_p + up(pb), o_e = o_t + up(tb), o_c = o_e + up(eb),
-                 o_err = o_c + 256, o_s = o_err + 256;
+    const size_t o_sw = up(jb), o_p = o_sw + up(swb), o_t = o_p + up(pb), o_pa = o_t + up(tb), o_tt = o_pa + up(pab),
+                 o_e = o_tt + up(ttb), o_c = o_e + up(eb), o_err = o_c + 256, o_s = o_err + 256;
     cudaStream_t st = nullptr;
     e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(e, "stream");
@@ -414,6 +594,8 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
     a.slots = dbuf + o_s;
     a.slot_elems = slot_elems;
     a.err = (int *)(dbuf + o_err);
+    a.passes = (const BatchPass *)(dbuf + o_pa);
+    a.tterms = (const BatchTileTerm *)(dbuf + o_tt);
     int err_flag = 0;
     e = copy_async(dbuf, jobs.data(), jb, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nsweeps)
@@ -422,6 +604,10 @@ static int32_t batch_run(int prec, std::vector<BatchCircuitIn> &circs, double *e
         e = copy_async(dbuf + o_p, prog.get(), nprog * sizeof(TileGate), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nterms)
         e = copy_async(dbuf + o_t, terms.get(), nterms * sizeof(BatchTerm), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && npass)
+        e = copy_async(dbuf + o_pa, passes.get(), npass * sizeof(BatchPass), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && ntt)
+        e = copy_async(dbuf + o_tt, tterms.get(), ntt * sizeof(BatchTileTerm), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dbuf + o_c, 0, 512, st);
     if (e == cudaSuccess) {
         k_batch_circuits<P, K, R><<<grid, BK::kThreads, BK::kSmem, st>>>(a);
