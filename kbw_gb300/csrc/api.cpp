@@ -620,7 +620,31 @@ static int32_t parse_hamiltonian(uint32_t n, const uint8_t *paulis, const uintpt
 }
 
 // <psi|H|psi> on the handle's current state (queue flushed by the caller).
+// True when every string of H is summed by a kernel that reads the
+// float-float resident form as is: the diagonal groups (x = 0) and the tiled
+// pair passes (no string too wide for a tile).
+static bool exp_reads_ff(const Sim &s, const std::vector<PauliString> &strs) {
+    const int K = pauli_tile_bits<double>();
+    if (s.n < (uint32_t)K) return false;
+    std::vector<uint64_t> xm;
+    for (const PauliString &t : strs)
+        if (t.x != 0) xm.push_back(t.x);
+    std::vector<size_t> wide;
+    plan_pauli_passes(s.n, K, xm, kMaxTerms, wide);
+    return wide.empty();
+}
+
+// Flush for exp_value: a float-float resident state stays in that form when
+// exp_value_core can read it (no conversion pass), else it goes to binary64.
+static cudaError_t settle_for_exp(Sim &s, const std::vector<PauliString> &strs) {
+    cudaError_t e = flush_queue(s);
+    if (e != cudaSuccess) return e;
+    if (s.ff_resident && !exp_reads_ff(s, strs)) return ensure_binary64(s);
+    return cudaSuccess;
+}
+
 static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs, double *out) {
+    const bool ff = s->ff_resident;  // (settle_for_exp left it so only when every kernel below reads that form)
     const size_t n_strings = strs.size();
     std::vector<size_t> order(n_strings);
     for (size_t k = 0; k < n_strings; k++) order[k] = k;
@@ -672,7 +696,7 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
             pass.nterms = (uint32_t)take.size();
             CUDA_TRY(dispatch(s, [&](auto *tp) {
                 using T = std::remove_pointer_t<decltype(tp)>;
-                return launch_pauli_tile<T>(s->state, s->n, false, pass, s->rs, s->stream);
+                return launch_pauli_tile<T>(s->state, s->n, ff, pass, s->rs, s->stream);
             }));
             CUDA_TRY(cudaMemcpyAsync(d_vals + slot_of.size(), s->rs.result, take.size() * 8,
                                      cudaMemcpyDeviceToDevice, s->stream));
@@ -704,7 +728,7 @@ static int32_t exp_value_core(kbwg_sim *s, const std::vector<PauliString> &strs,
         g.nterms = (uint32_t)idx.size();
         CUDA_TRY(dispatch(s, [&](auto *tp) {
             using T = std::remove_pointer_t<decltype(tp)>;
-            return launch_pauli_group<T>(s->state, s->n, g, s->rs, s->stream);
+            return launch_pauli_group<T>(s->state, s->n, g, s->rs, s->stream, ff);
         }));
         CUDA_TRY(cudaMemcpyAsync(d_vals + slot_of.size(), s->rs.result, idx.size() * 8, cudaMemcpyDeviceToDevice,
                                  s->stream));
@@ -762,7 +786,7 @@ int32_t kbwg_exp_value(kbwg_sim *s, const uint8_t *paulis, const uintptr_t *qubi
     std::vector<PauliString> strs;
     int32_t r = parse_hamiltonian(s->n, paulis, qubits, offsets, coefficients, n_strings, strs);
     if (r) return r;
-    CUDA_TRY(settle(*s));
+    CUDA_TRY(settle_for_exp(*s, strs));
     return exp_value_core(s, strs, out);
     GUARD_END
 }
@@ -817,7 +841,7 @@ int32_t kbwg_param_shift_gradient(kbwg_sim *s, const kbwg_gate *gates, uintptr_t
         s->queue.clear();
         CUDA_TRY(init_state(*s));
         s->queue = circ;
-        CUDA_TRY(settle(*s));
+        CUDA_TRY(settle_for_exp(*s, strs));
         return exp_value_core(s, strs, e);
     };
     r = evaluate(fwd, energy);

@@ -78,9 +78,11 @@ struct PauliGroup {
     double factor[kMaxTerms];   // +-1 (x == 0) or +-2 (pair form)
     uint32_t use_im[kMaxTerms]; // pair form: Im(conj(a_s) a_{s^x}) instead of Re
 };
+// ff_resident: the state is in the float-float resident form (complex128,
+// diagonal groups only).
 template <class T>
 cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, const ReduceScratch &rs,
-                               cudaStream_t s);
+                               cudaStream_t s, bool ff_resident = false);
 
 // Pair-form Pauli strings with different flip masks in one pass: a tile of
 // 2^K amplitudes (local bits 0..l-1 = qubits 0..l-1, l..K-1 = qubits hq[])

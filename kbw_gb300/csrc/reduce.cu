@@ -480,16 +480,26 @@ __global__ void __launch_bounds__(kReduceThreads)
 // (-1)^{|s & z|} = (-1)^{|(b | lane) & z|} * (-1)^{|u & zu|}, zu = (z >> 5) & 15.
 // Each thread forms the 16-point Walsh-Hadamard transform W of its
 // probabilities p_u (64 adds) and every term adds +-W[zu]: about 4 + nt/16
-// additions per amplitude instead of nt.  Probabilities and sums are binary64
-// for complex128 data and float-float (error-free products) for complex64.
+// additions per amplitude instead of nt.  Probabilities and sums are
+// float-float: error-free products of the complex64 parts, and for complex128
+// a float-float dot product of the amplitude split into float-float (binary64
+// storage) or read as is (the float-float resident form) -- FP32-pipe work
+// instead of GB300's slow FP64 pipe, ~2^-48 relative per operation.
 template <class T> struct DiagArith;
 template <> struct DiagArith<double> {
-    using V = double;
-    static __device__ __forceinline__ V zero() { return 0.0; }
-    static __device__ __forceinline__ V prob(cx<double> a) { return __fma_rn(a.re, a.re, __dmul_rn(a.im, a.im)); }
-    static __device__ __forceinline__ V add(V a, V b) { return __dadd_rn(a, b); }
-    static __device__ __forceinline__ V sub(V a, V b) { return __dsub_rn(a, b); }
-    static __device__ __forceinline__ double to_d(V a) { return a; }
+    using V = ff::f2;
+    static __device__ __forceinline__ V zero() { return V{0.f, 0.f}; }
+    static __device__ __forceinline__ V prob(cx<double> a) {
+        const ff::f2 re = ff::from_double(a.re), im = ff::from_double(a.im);
+        return ff::dot2(re, re, im, im);
+    }
+    static __device__ __forceinline__ V prob(float4 f) {  // re.hi, im.hi, re.lo, im.lo
+        const ff::f2 re{f.x, f.z}, im{f.y, f.w};
+        return ff::dot2(re, re, im, im);
+    }
+    static __device__ __forceinline__ V add(V a, V b) { return ff::add(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return ff::sub(a, b); }
+    static __device__ __forceinline__ double to_d(V a) { return (double)a.h + (double)a.l; }
 };
 template <> struct DiagArith<float> {
     using V = ff::f2;
@@ -508,9 +518,9 @@ template <> struct DiagArith<float> {
 constexpr int kDiagRun = 16;                   // amplitudes per thread per run
 constexpr int kDiagWarpSpan = 32 * kDiagRun;  // 512 consecutive amplitudes per warp
 
-template <class T>
+template <class T, bool kFF>
 __global__ void __launch_bounds__(kReduceThreads, 2)
-    k_pauli_diag(const cx<T> *__restrict__ st, uint32_t n, PauliGroup g, ReduceScratch rs) {
+    k_pauli_diag(const void *__restrict__ st, uint32_t n, PauliGroup g, ReduceScratch rs) {
     using A = DiagArith<T>;
     using V = typename A::V;
     __shared__ V wsh[kReduceThreads / 32][kDiagRun][32];
@@ -530,7 +540,12 @@ __global__ void __launch_bounds__(kReduceThreads, 2)
         const uint64_t b = r * kDiagWarpSpan;
         V p[kDiagRun];
 #pragma unroll
-        for (int u = 0; u < kDiagRun; u++) p[u] = A::prob(st[b + lane + 32 * u]);
+        for (int u = 0; u < kDiagRun; u++) {
+            if constexpr (kFF)
+                p[u] = A::prob(reinterpret_cast<const float4 *>(st)[b + lane + 32 * u]);
+            else
+                p[u] = A::prob(reinterpret_cast<const cx<T> *>(st)[b + lane + 32 * u]);
+        }
 #pragma unroll
         for (int h = 1; h < kDiagRun; h <<= 1) {
 #pragma unroll
@@ -572,11 +587,21 @@ __global__ void __launch_bounds__(kReduceThreads, 2)
 
 template <class T>
 cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, const ReduceScratch &rs,
-                               cudaStream_t s) {
-    if (g.x == 0 && (1ull << n) >= (uint64_t)kDiagWarpSpan)
-        k_pauli_diag<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, n, g, rs);
-    else
+                               cudaStream_t s, bool ff_resident) {
+    if (ff_resident && !(sizeof(T) == 8 && g.x == 0 && (1ull << n) >= (uint64_t)kDiagWarpSpan))
+        return cudaErrorInvalidValue;  // (only the diagonal form reads the float-float resident state)
+    if (g.x == 0 && (1ull << n) >= (uint64_t)kDiagWarpSpan) {
+        if constexpr (sizeof(T) == 8) {
+            if (ff_resident)
+                k_pauli_diag<T, true><<<kReduceBlocks, kReduceThreads, 0, s>>>(st, n, g, rs);
+            else
+                k_pauli_diag<T, false><<<kReduceBlocks, kReduceThreads, 0, s>>>(st, n, g, rs);
+        } else {
+            k_pauli_diag<T, false><<<kReduceBlocks, kReduceThreads, 0, s>>>(st, n, g, rs);
+        }
+    } else {
         k_pauli_group<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, n, g, rs);
+    }
     count_launch();
     return cudaGetLastError();
 }
@@ -1068,7 +1093,7 @@ namespace kbwg {
     template cudaError_t launch_collapse<T>(void *, uint32_t, const MeasureCtl *, uint64_t, uint64_t, double,   \
                                             cudaStream_t);                                                    \
     template cudaError_t launch_pauli_group<T>(const void *, uint32_t, const PauliGroup &, const ReduceScratch &, \
-                                               cudaStream_t);                                                 \
+                                               cudaStream_t, bool);                                           \
     template cudaError_t launch_pauli_tile<T>(const void *, uint32_t, bool, const PauliTilePass &,               \
                                               const ReduceScratch &, cudaStream_t);                           \
     template cudaError_t launch_dump_count<T>(const void *, uint32_t, uint64_t *, cudaStream_t);               \
