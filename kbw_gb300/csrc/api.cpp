@@ -379,12 +379,16 @@ int32_t kbwg_measure_p1(kbwg_sim *s, uintptr_t target, double *p1) {
     ENTER(s);
     if (!p1) return fail(KBWG_EINVAL, "null output");
     if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
-    CUDA_TRY(settle(*s));
+    CUDA_TRY(flush_queue(*s));  // (a float-float resident state is read as is)
     const uint64_t bit = 1ull << target;
-    CUDA_TRY(dispatch(s, [&](auto *tp) {
-        using T = std::remove_pointer_t<decltype(tp)>;
-        return launch_masked_norm<T>(s->state, s->n, bit, bit, s->rs, s->stream);
-    }));
+    if (s->ff_resident) {
+        CUDA_TRY(launch_masked_norm_ff(s->state, s->n, bit, bit, s->rs, s->stream));
+    } else {
+        CUDA_TRY(dispatch(s, [&](auto *tp) {
+            using T = std::remove_pointer_t<decltype(tp)>;
+            return launch_masked_norm<T>(s->state, s->n, bit, bit, s->rs, s->stream);
+        }));
+    }
     CUDA_TRY(copy_async(s->h_result, s->rs.result, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     *p1 = s->h_result[0];
@@ -396,12 +400,16 @@ int32_t kbwg_measure_collapse(kbwg_sim *s, uintptr_t target, bool result, double
     GUARD_BEGIN
     ENTER(s);
     if (target >= s->n) return fail(KBWG_EINVAL, "target qubit out of range");
-    CUDA_TRY(settle(*s));
+    CUDA_TRY(flush_queue(*s));  // (a float-float resident state is collapsed as is)
     const uint64_t bit = 1ull << target;
-    CUDA_TRY(dispatch(s, [&](auto *tp) {
-        using T = std::remove_pointer_t<decltype(tp)>;
-        return launch_collapse<T>(s->state, s->n, nullptr, bit, result ? bit : 0ull, p, s->stream);
-    }));
+    if (s->ff_resident) {
+        CUDA_TRY(launch_collapse_ff(s->state, s->n, nullptr, bit, result ? bit : 0ull, p, s->stream));
+    } else {
+        CUDA_TRY(dispatch(s, [&](auto *tp) {
+            using T = std::remove_pointer_t<decltype(tp)>;
+            return launch_collapse<T>(s->state, s->n, nullptr, bit, result ? bit : 0ull, p, s->stream);
+        }));
+    }
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return KBWG_OK;
     GUARD_END
@@ -421,7 +429,7 @@ int32_t kbwg_measure(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, c
     }
     *result = 0;
     if (n_qubits == 0) return KBWG_OK;
-    CUDA_TRY(settle(*s));
+    CUDA_TRY(flush_queue(*s));  // (a float-float resident state is measured as is)
     MeasureCtl &c = *s->h_ctl;
     memset(&c, 0, sizeof c);
     c.scale2 = 1.0;
@@ -430,14 +438,20 @@ int32_t kbwg_measure(kbwg_sim *s, const uintptr_t *qubits, uintptr_t n_qubits, c
         c.draws[k] = draws ? draws[k] : next_draw(*s);
     }
     CUDA_TRY(copy_async(s->d_ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(dispatch(s, [&](auto *tp) {
-        using T = std::remove_pointer_t<decltype(tp)>;
-        for (uint32_t k = 0; k < n_qubits; k++) {
-            cudaError_t e = launch_measure_step<T>(s->state, s->n, s->d_ctl, k, s->rs, s->stream);
-            if (e != cudaSuccess) return e;
-        }
-        return launch_collapse<T>(s->state, s->n, s->d_ctl, 0, 0, 0.0, s->stream);
-    }));
+    if (s->ff_resident) {
+        for (uint32_t k = 0; k < n_qubits; k++)
+            CUDA_TRY(launch_measure_step_ff(s->state, s->n, s->d_ctl, k, s->rs, s->stream));
+        CUDA_TRY(launch_collapse_ff(s->state, s->n, s->d_ctl, 0, 0, 0.0, s->stream));
+    } else {
+        CUDA_TRY(dispatch(s, [&](auto *tp) {
+            using T = std::remove_pointer_t<decltype(tp)>;
+            for (uint32_t k = 0; k < n_qubits; k++) {
+                cudaError_t e = launch_measure_step<T>(s->state, s->n, s->d_ctl, k, s->rs, s->stream);
+                if (e != cudaSuccess) return e;
+            }
+            return launch_collapse<T>(s->state, s->n, s->d_ctl, 0, 0, 0.0, s->stream);
+        }));
+    }
     CUDA_TRY(copy_async(&c, s->d_ctl, sizeof c, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     *result = c.result;

@@ -80,6 +80,14 @@ struct PauliGroup {
 };
 // ff_resident: the state is in the float-float resident form (complex128,
 // diagonal groups only).
+// Float-float resident complex128 state (sweeps leave it so): the masked
+// norm, one measurement step and the collapse read and write that form.
+cudaError_t launch_masked_norm_ff(const void *st, uint32_t n, uint64_t M, uint64_t V, const ReduceScratch &rs,
+                                  cudaStream_t s);
+cudaError_t launch_measure_step_ff(const void *st, uint32_t n, MeasureCtl *ctl, uint32_t step,
+                                   const ReduceScratch &rs, cudaStream_t s);
+cudaError_t launch_collapse_ff(void *st, uint32_t n, const MeasureCtl *ctl, uint64_t M, uint64_t V, double p,
+                               cudaStream_t s);
 template <class T>
 cudaError_t launch_pauli_group(const void *st, uint32_t n, const PauliGroup &g, const ReduceScratch &rs,
                                cudaStream_t s, bool ff_resident = false);

@@ -205,6 +205,42 @@ cudaError_t launch_masked_norm(const void *st, uint32_t n, uint64_t M, uint64_t 
     return cudaGetLastError();
 }
 
+// The same over the float-float resident form of a complex128 state
+// (re.hi, im.hi, re.lo, im.lo per amplitude): |a|^2 as a float-float dot
+// product, summed per thread in float-float (FP32-pipe work), then in binary64.
+__device__ __forceinline__ double masked_norm_body_ff(const float4 *__restrict__ st, uint64_t count, uint64_t M,
+                                                      uint64_t V) {
+    ff::f2 acc{0.f, 0.f};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const float4 f = st[insert_zeros(i, M) | V];
+        const ff::f2 re{f.x, f.z}, im{f.y, f.w};
+        acc = ff::add(acc, ff::dot2(re, re, im, im));
+    }
+    return block_sum((double)acc.h + (double)acc.l);
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    k_masked_norm_ff(const float4 *__restrict__ st, uint64_t count, uint64_t M, uint64_t V, ReduceScratch rs) {
+    const double v = masked_norm_body_ff(st, count, M, V);
+    if (threadIdx.x == 0) rs.partials[blockIdx.x] = v;
+    if (last_block(rs.ticket)) {
+        const double t = sum_partials(rs.partials, gridDim.x, 1, 0);
+        if (threadIdx.x == 0) {
+            rs.result[0] = t;
+            *rs.ticket = 0;
+        }
+    }
+}
+
+cudaError_t launch_masked_norm_ff(const void *st, uint32_t n, uint64_t M, uint64_t V, const ReduceScratch &rs,
+                                  cudaStream_t s) {
+    const uint64_t count = 1ull << (n - __builtin_popcountll(M));
+    k_masked_norm_ff<<<kReduceBlocks, kReduceThreads, 0, s>>>((const float4 *)st, count, M, V, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ---- distance between two states ----------------------------------------------
 // partials: sum |a - b|^2 and sum |b|^2 (two values per block).
 template <class T>
@@ -306,13 +342,17 @@ cudaError_t launch_overlap(const void *a, int prec_a, const void *b, int prec_b,
 }
 
 // ---- sequential measurement step ------------------------------------------
-template <class T>
+template <class T, bool kFF = false>
 __global__ void __launch_bounds__(kReduceThreads)
-    k_measure_step(const cx<T> *__restrict__ st, uint32_t n, MeasureCtl *ctl, uint32_t step, ReduceScratch rs) {
+    k_measure_step(const void *__restrict__ st, uint32_t n, MeasureCtl *ctl, uint32_t step, ReduceScratch rs) {
     const uint64_t bit = 1ull << ctl->qubit[step];
     const uint64_t M = ctl->M | bit, V = ctl->V | bit;
     const uint64_t count = 1ull << (n - __popcll(M));
-    const double v = masked_norm_body<T>(st, count, M, V);
+    double v;
+    if constexpr (kFF)
+        v = masked_norm_body_ff((const float4 *)st, count, M, V);
+    else
+        v = masked_norm_body<T>((const cx<T> *)st, count, M, V);
     if (threadIdx.x == 0) rs.partials[blockIdx.x] = v;
     if (last_block(rs.ticket)) {
         const double s1 = sum_partials(rs.partials, gridDim.x, 1, 0);
@@ -342,7 +382,14 @@ __global__ void __launch_bounds__(kReduceThreads)
 template <class T>
 cudaError_t launch_measure_step(const void *st, uint32_t n, MeasureCtl *ctl, uint32_t step,
                                 const ReduceScratch &rs, cudaStream_t s) {
-    k_measure_step<T><<<kReduceBlocks, kReduceThreads, 0, s>>>((const cx<T> *)st, n, ctl, step, rs);
+    k_measure_step<T><<<kReduceBlocks, kReduceThreads, 0, s>>>(st, n, ctl, step, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_measure_step_ff(const void *st, uint32_t n, MeasureCtl *ctl, uint32_t step,
+                                   const ReduceScratch &rs, cudaStream_t s) {
+    k_measure_step<double, true><<<kReduceBlocks, kReduceThreads, 0, s>>>(st, n, ctl, step, rs);
     count_launch();
     return cudaGetLastError();
 }
@@ -384,6 +431,60 @@ __global__ void __launch_bounds__(256)
         }
         st[s] = a;
     }
+}
+
+// The collapse of a float-float resident state: each kept amplitude's parts
+// times the binary64 factors 1/sqrt(P) in float-float, one per collapse, in
+// order.
+__global__ void __launch_bounds__(256)
+    k_collapse_ff(float4 *__restrict__ st, uint64_t ns, const MeasureCtl *ctl, uint64_t M, uint64_t V, double p) {
+    __shared__ float ph[64], pl[64];
+    __shared__ uint64_t sM, sV;
+    __shared__ uint32_t nf;
+    if (threadIdx.x == 0) {
+        if (ctl) {
+            sM = ctl->M;
+            sV = ctl->V;
+            nf = ctl->steps;
+        } else {
+            sM = M;
+            sV = V;
+            nf = 1;
+        }
+    }
+    if (threadIdx.x < 64) {
+        const ff::f2 f = ff::split_constant(ctl ? ctl->p[threadIdx.x] : p);
+        ph[threadIdx.x] = f.h;
+        pl[threadIdx.x] = f.l;
+    }
+    __syncthreads();
+    const uint64_t m = sM, v = sV;
+    const uint32_t k = nf;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((s & m) == v) {
+            a = st[s];
+            ff::f2 re{a.x, a.z}, im{a.y, a.w};
+            for (uint32_t j = 0; j < k; j++) {
+                const ff::f2 f{ph[j], pl[j]};
+                re = ff::mul(re, f);
+                im = ff::mul(im, f);
+            }
+            a = make_float4(re.h, im.h, re.l, im.l);
+        }
+        st[s] = a;
+    }
+}
+
+cudaError_t launch_collapse_ff(void *st, uint32_t n, const MeasureCtl *ctl, uint64_t M, uint64_t V, double p,
+                               cudaStream_t s) {
+    const uint64_t ns = 1ull << n;
+    uint64_t g = (ns + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_collapse_ff<<<(unsigned)g, 256, 0, s>>>((float4 *)st, ns, ctl, M, V, p);
+    count_launch();
+    return cudaGetLastError();
 }
 
 template <class T>

@@ -389,9 +389,11 @@ def test_fast_c128_many_hadamards_rescale():
 
 def test_fast_c128_resident_format_transitions():
     """The float-float handle keeps its state in float-float form between
-    sweeps and returns to binary64 for every other operation: interleave
-    gates with every kind of read, a swap (format-agnostic), a collapse,
-    set_state and clear, and follow the restated Dense<f64> throughout."""
+    sweeps; exp_value, measure_p1, collapse and measurement read (and
+    write) that form as is, the other operations return it to binary64:
+    interleave gates with every kind of read, a swap (format-agnostic), a
+    collapse, a partial measurement, set_state and clear, and follow the
+    restated Dense<f64> throughout."""
     n = 14
     sim = DenseGB300(n, "c128", fast_c128=True)
     ref = oracle.OracleDense(n, "c128")
@@ -411,6 +413,11 @@ def test_fast_c128_resident_format_transitions():
     sim.measure_collapse(5, True, 1.0 / math.sqrt(p))
     ref.measure_collapse(5, True, 1.0 / math.sqrt(p))
     step(C.random_circuit(n, 100, 74))
+    draws = C.uniform_draws(4, 9)
+    assert sim.measure([1, 7, 12, 3], draws) == ref.measure([1, 7, 12, 3], draws)
+    step(C.random_circuit(n, 80, 76))
+    assert rel_err(sim.state(), ref.state()) < 1e-12
+    step(C.random_circuit(n, 40, 77))
     h = C.tfim_ring(n) + [(0.3, [(C.PAULI_Y, 1), (C.PAULI_Z, 6)])]
     assert abs(sim.exp_value(h) - ref.exp_value(h)) < 1e-11
     step(C.random_circuit(n, 60, 75))
