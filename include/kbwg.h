@@ -79,7 +79,8 @@ enum {
  * and neither has this engine below 40 (KBWG_EQUBITS above): the device's
  * memory decides (KBWG_ENOMEM), one GB300 holding 34 qubits in complex128 or
  * 35 in complex64 (256 GiB).  Above 32 qubits gates run in the default tile geometry
- * with 64-bit state indices; the adjoint gradient stays at 32 qubits. */
+ * with 64-bit state indices; the adjoint gradient too, as far as memory holds
+ * its state, lambda and checkpoints (33 qubits in complex64 on one GB300). */
 int32_t kbwg_new(uintptr_t num_qubits, int32_t precision, uint32_t flags, kbwg_sim **out);
 
 /* Drop of the backend (ket frees its QPUConfig, src/c_api.rs:124). */

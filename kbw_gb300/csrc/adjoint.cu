@@ -342,7 +342,8 @@ __global__ void __launch_bounds__(256) k_inner_re(const cx<T> *__restrict__ a, c
     }
 }
 
-template <class P, int K, int R>
+// W: registers above 32 qubits (the gates read bits of the 64-bit tile base).
+template <class P, int K, int R, bool W = false>
 __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
     k_adjoint(typename P::Mem *__restrict__ phi, typename P::Mem *__restrict__ lam, const __grid_constant__ AdjParams a) {
     using Amp = typename P::Amp;
@@ -456,8 +457,9 @@ __global__ void __launch_bounds__(AdjKernel<P, K, R>::kThreads, 2)
                         slot = G::wadd(slot, w);
                     }
                 }
-                tile_gate<P, K, R>(g, vp, R0, F, base);
-                tile_gate<P, K, R>(g, vl, R0, F, base);
+                using B = typename pick_t<W, uint64_t, uint32_t>::type;
+                tile_gate<P, K, R, B>(g, vp, R0, F, (B)base);
+                tile_gate<P, K, R, B>(g, vl, R0, F, (B)base);
             }
             g0 = g1;
         }
@@ -709,7 +711,11 @@ static cudaError_t run_segment(Sim &s, AdjScratch &sc, std::vector<RevSweep> &sw
             void *args[] = {(void *)&ph, (void *)&la, (void *)&r.a};
             e = cudaLaunchKernel(r.spec, dim3((unsigned)grid), dim3(AK::kThreads), args, AK::kSmem, s.stream);
         } else {
-            k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)sc.lam,
+            if (s.n > 32)
+                k_adjoint<P, K, R, true><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>(
+                    (Mem *)s.state, (Mem *)sc.lam, r.a);
+            else
+                k_adjoint<P, K, R><<<(unsigned)grid, AK::kThreads, AK::kSmem, s.stream>>>((Mem *)s.state, (Mem *)sc.lam,
                                                                                     r.a);
             e = cudaGetLastError();
         }
@@ -953,7 +959,8 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
     int dev = 0, num_sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = ensure_smem_limit((const void *)k_adjoint<P, K, R>, AK::kSmem);
+    const void *kadj = s.n > 32 ? (const void *)k_adjoint<P, K, R, true> : (const void *)k_adjoint<P, K, R>;
+    if (e == cudaSuccess) e = ensure_smem_limit(kadj, AK::kSmem);
     if (e != cudaSuccess) return fail_cuda(e, "device query");
     // scratch (kept from an earlier call when it is there)
     if (sc.sb != sb) sc.release_states();
@@ -1035,7 +1042,7 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
     }
     // one grid per kernel: as many CTAs as fit (the partials buffer holds 8 per SM)
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<P, K, R>, AK::kThreads, AK::kSmem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kadj, AK::kThreads, AK::kSmem);
     if (e != cudaSuccess) return fail_cuda(e, "occupancy");
     const uint64_t tiles = 1ull << (s.n - K);
     std::vector<std::pair<const void *, uint64_t>> grids;
@@ -1153,10 +1160,8 @@ size_t jit_check_adjoint(const Sim &s, const std::vector<GateDesc> &fwd, const s
 int32_t adjoint_gradient(Sim &s, const std::vector<GateDesc> &fwd, const std::vector<double> &angles,
                          const std::vector<int> &gtype, const std::vector<PauliString> &H, double *energy,
                          std::vector<double> &grad_per_gate, uint32_t max_ckpt) {
-    if (s.n > 32) {  // the reverse sweeps index with 32 bits (and need three states)
-        set_error(KBWG_EUNSUPPORTED, "adjoint: at most 32 qubits");
-        return KBWG_EUNSUPPORTED;
-    }
+    // (above 32 qubits the reverse sweeps read gate bits of a 64-bit tile
+    // base; memory decides how far: the state, lambda and the checkpoints)
     if (s.n < (uint32_t)AdjCfg<float>::K || (s.prec && s.n < (uint32_t)AdjCfg<double>::K)) {
         set_error(KBWG_EUNSUPPORTED, "adjoint: needs at least 12 qubits (complex64) or 11 (complex128)");
         return KBWG_EUNSUPPORTED;

@@ -225,3 +225,51 @@ def test_adjoint_24q_slice_vs_oracle_param_shift_and_fd():
         gs = grad[picks]
         assert np.max(np.abs(gs - ps)) < tol, (prec, fast, np.max(np.abs(gs - ps)))
         assert np.max(np.abs(gs - fd)) < tol_fd, (prec, fast, np.max(np.abs(gs - fd)))
+
+
+def test_adjoint_above_32_qubits_vs_finite_differences():
+    # 33 qubits in complex64 (64 GiB per state: the state, lambda and one
+    # checkpoint): gates on qubit 32 as targets (parameterised and diagonal),
+    # as controls, and diagonal gates whose target lies outside every tile.
+    # The energy must equal exp_value after the circuit, and the gradient of
+    # the parameters on those gates central differences of exp_value (the
+    # forward sweeps and reductions, independent of the reverse sweeps).
+    import gc
+    gc.collect()
+    n, L = 33, 2
+    params = C.hea_params(n, L, 11)
+    circ = C.hea(n, L, params)
+    pidx = C.hea_param_index(n, L)
+    k = len(params)
+    extra = [(C.P, 32, (), 0.7), (C.RY, 5, (32,), -0.4), (C.RZ, 32, (3,), 1.1), (C.RX, 32, (), 0.3),
+             (C.H, 32, (), 0.0), (C.RZ, 32, (), -0.9), (C.RY, 31, (), 0.5), (C.X, 0, (32,), 0.0)]
+    checked = []
+    for g in extra:
+        circ.append(g)
+        if g[0] in C.PARAMETRIC:
+            pidx.append(k)
+            checked.append((len(circ) - 1, k))
+            k += 1
+        else:
+            pidx.append(-1)
+    ham = C.tfim_ring(n) + [(0.6, [(C.PAULI_X, 32), (C.PAULI_Z, 0)]), (-0.3, [(C.PAULI_Z, 32)])]
+    sim = DenseGB300(n, "c64")
+    e, g = sim.adjoint_gradient(circ, pidx, k, ham, max_checkpoints=1)
+
+    def energy(c):
+        sim.clear()
+        sim.apply(c)
+        return sim.exp_value(ham)
+
+    assert abs(e - energy(circ)) < 5e-5
+    h = 5e-3
+    for gi, p in checked[:4] + [(i, pidx[i]) for i in (0, 31, 32, 65) if pidx[i] >= 0][:3]:
+        kind, t, c, a = circ[gi]
+        plus, minus = list(circ), list(circ)
+        plus[gi] = (kind, t, c, a + h)
+        minus[gi] = (kind, t, c, a - h)
+        fd = (energy(plus) - energy(minus)) / (2 * h)
+        assert abs(g[p] - fd) < 2e-3, (gi, g[p], fd)
+    sim.close()
+    del sim
+    gc.collect()
