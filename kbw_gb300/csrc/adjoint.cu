@@ -1000,16 +1000,15 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         e = flush_queue(s);
         if (e != cudaSuccess) return fail_cuda(e, "forward");
         if (seg + 1 < S) {
-            // checkpoints take the reverse sweeps' form: float-float copies,
-            // or binary64 (a float-float forward state is exported)
+            // checkpoints are copies in the reverse sweeps' form (float-float
+            // for FF2, binary64 otherwise)
             if (kFF && !s.ff_resident) {
                 e = launch_ff_convert(s.state, s.n, true, s.stream);
                 if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
                 s.ff_resident = true;
             }
-            e = (!kFF && s.ff_resident)
-                    ? launch_ff_export(s.state, sc.ckpt[seg], s.n, s.stream)
-                    : cudaMemcpyAsync(sc.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
+            if (!kFF) e = ensure_binary64(s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(sc.ckpt[seg], s.state, sb, cudaMemcpyDeviceToDevice, s.stream);
             if (e != cudaSuccess) return fail_cuda(e, "checkpoint");
         }
     }

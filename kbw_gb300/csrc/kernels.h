@@ -36,8 +36,7 @@ template <class T> cudaError_t launch_gate1(void *st, uint32_t n, const GateDesc
 template <class T> cudaError_t launch_init(void *st, uint32_t n, cudaStream_t s);
 // complex128 storage: binary64 -> float-float pairs (to_ff) or back, in place.
 cudaError_t launch_ff_convert(void *st, uint32_t n, bool to_ff, cudaStream_t s);
-// Binary64 copy of a float-float state into dst (the source is unchanged).
-cudaError_t launch_ff_export(const void *src, void *dst, uint32_t n, cudaStream_t s);
+// |0...0> in the float-float resident form.
 cudaError_t launch_init_ff(void *st, uint32_t n, cudaStream_t s);
 // One CTA runs the tile kernels' bounded wait on a barrier nothing completes.
 cudaError_t launch_wait_probe(int *err, uint32_t spins, cudaStream_t s);

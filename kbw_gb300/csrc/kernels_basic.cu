@@ -68,16 +68,6 @@ __global__ void __launch_bounds__(256) k_ff_convert(cx<double> *__restrict__ st,
     }
 }
 
-// Out-of-place float-float -> binary64 copy (the source keeps its form).
-__global__ void __launch_bounds__(256) k_ff_export(const float4 *__restrict__ src, cx<double> *__restrict__ dst,
-                                                   uint64_t ns) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
-        const float4 f = src[s];
-        dst[s] = cx<double>{ff::to_double(ff::f2{f.x, f.z}), ff::to_double(ff::f2{f.y, f.w})};
-    }
-}
-
 // In-place exchange of physical qubits a < b: amplitudes with (bit a, bit b)
 // = (1, 0) and (0, 1) trade places; the others stay.  One thread per swapped
 // pair; 2^(n-2) pairs.
@@ -135,12 +125,6 @@ cudaError_t launch_ff_convert(void *st, uint32_t n, bool to_ff, cudaStream_t s) 
     return cudaGetLastError();
 }
 
-cudaError_t launch_ff_export(const void *src, void *dst, uint32_t n, cudaStream_t s) {
-    const uint64_t ns = 1ull << n;
-    k_ff_export<<<grid_for(ns, 256, 152 * 16), 256, 0, s>>>((const float4 *)src, (cx<double> *)dst, ns);
-    count_launch();
-    return cudaGetLastError();
-}
 
 template <class T>
 cudaError_t launch_swap(void *st, uint32_t n, uint32_t a, uint32_t b, cudaStream_t s) {
