@@ -229,3 +229,36 @@ def test_specialised_adjoint_kernels_compile(lib, prec, flags):
         raise
     assert sweeps > 0
     assert failed == 0, N.jit_last_error()
+
+
+def test_batch_circuits_validation(lib):
+    """kbwg_batch_circuits_exp_value checks every circuit (on all host
+    cores) before any device work: status codes for bad qubit counts, gates,
+    Pauli codes and qubits, a qubit named twice in a string, and offsets that
+    decrease; the first bad circuit in index order decides the code."""
+    from kbw_gb300.dense import batch_circuits_prepare, batch_circuits_run
+    assert len(batch_circuits_run(batch_circuits_prepare([]))) == 0
+    good = (4, [(C.H, 0, (), 0.0), (C.X, 1, (0,), 0.0)], [(1.0, [(C.PAULI_Z, 1)])])
+    cases = [
+        ([(25, [], [])], N.EQUBITS),
+        ([(0, [], [])], N.EQUBITS),
+        ([good, (3, [(C.X, 3, (), 0.0)], [])], N.EINVAL),             # target out of range
+        ([good, (3, [(C.X, 1, (1,), 0.0)], [])], N.EINVAL),           # target among its controls
+        ([good, (3, [(C.X, 1, (5,), 0.0)], [])], N.EINVAL),           # control out of range
+        ([good, (3, [(8, 1, (), 0.0)], [])], N.EINVAL),               # no such gate kind
+        ([good, (3, [], [(1.0, [(4, 1)])])], N.EINVAL),               # no such Pauli code
+        ([good, (3, [], [(1.0, [(C.PAULI_X, 3)])])], N.EINVAL),       # qubit out of range
+        ([good, (3, [], [(1.0, [(C.PAULI_Z, 1), (C.PAULI_X, 1)])])], N.EINVAL),  # qubit twice
+        ([good, (3, [(C.X, 3, (), 0.0)], []), (30, [], [])], N.EINVAL),  # circuit 1 before circuit 2
+        ([good, (30, [], []), (3, [(C.X, 3, (), 0.0)], [])], N.EQUBITS),
+    ]
+    for circs, code in cases:
+        with pytest.raises(N.KbwgError) as e:
+            batch_circuits_run(batch_circuits_prepare(circs))
+        assert e.value.code == code, (circs, e.value)
+    # decreasing offsets (within the arrays: circuit 1's range is [2, 1))
+    packed = batch_circuits_prepare([good, good])
+    packed["goff"][2] = 1
+    with pytest.raises(N.KbwgError) as e:
+        batch_circuits_run(packed)
+    assert e.value.code == N.EINVAL
