@@ -285,6 +285,90 @@ __global__ void __launch_bounds__(256) k_apply_group_ff(const ff2::v2 *__restric
     }
 }
 
+// The same runs for complex64 states (float arithmetic; the coefficients are
+// the high parts rh/ih): each thread keeps its 2^K/256 amplitudes u = tid +
+// 256 i in registers, the strings run in the outer loop (their fields read
+// once per tile), signs are counted per amplitude and partners summed per run.
+__global__ void __launch_bounds__(256) k_apply_tile_f32(const cx<float> *__restrict__ phi, cx<float> *__restrict__ lam,
+                                                        uint32_t n, const __grid_constant__ ApplyTilePassFF p) {
+    constexpr int K = kApplyTileBits, NA = (1 << K) / 256;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<float> *tile = reinterpret_cast<cx<float> *>(smem_raw);
+    const uint32_t l = p.l, m = p.m;
+    uint64_t *chunk_off = reinterpret_cast<uint64_t *>(smem_raw + (sizeof(cx<float>) << K));
+    for (uint32_t c = threadIdx.x; c < (1u << m); c += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < m; j++) off |= (uint64_t)((c >> j) & 1u) << p.hq[j];
+        chunk_off[c] = off;
+    }
+    const uint64_t tiles = 1ull << (n - K);
+    const uint32_t lowmask = (1u << l) - 1u;
+    __syncthreads();
+    for (uint64_t tau = blockIdx.x; tau < tiles; tau += gridDim.x) {
+        uint64_t base = tau << l;
+        for (uint32_t j = 0; j < m; j++) {
+            const uint64_t low = (1ull << p.hq[j]) - 1;
+            base = ((base & ~low) << 1) | (base & low);
+        }
+        cx<float> self[NA];
+#pragma unroll
+        for (int i = 0; i < NA; i++) {
+            const uint32_t u = threadIdx.x + 256u * (uint32_t)i;
+            self[i] = phi[base + chunk_off[u >> l] + (u & lowmask)];
+            tile[u] = self[i];
+        }
+        __syncthreads();
+        float ar[NA], ai[NA], rr[NA], ri[NA];
+        int cnt[NA];
+#pragma unroll
+        for (int i = 0; i < NA; i++) ar[i] = ai[i] = rr[i] = ri[i] = 0.f, cnt[i] = 0;
+        for (uint32_t k = 0; k < p.nterms; k++) {  // (branches depend on the string only: uniform)
+            const ApplyTileTermFF t = p.t[k];
+            const uint32_t op = (uint32_t)__popcll(base & t.zo) & 1u;
+#pragma unroll
+            for (int i = 0; i < NA; i++) {
+                const uint32_t u = threadIdx.x + 256u * (uint32_t)i, src = u ^ t.xl;
+                const bool neg = (((uint32_t)__popc(src & t.zl) + op) & 1u) != 0u;
+                if (t.cat == 0u) {
+                    cnt[i] += neg ? -1 : 1;
+                    if (t.last) {
+                        const float w = (float)cnt[i] * t.rh;
+                        ar[i] += w * self[i].re;
+                        ai[i] += w * self[i].im;
+                        cnt[i] = 0;
+                    }
+                } else if (t.cat == 1u) {
+                    const cx<float> a = tile[src];
+                    rr[i] += neg ? -a.re : a.re;
+                    ri[i] += neg ? -a.im : a.im;
+                    if (t.last) {
+                        ar[i] += t.rh * rr[i];
+                        ai[i] += t.rh * ri[i];
+                        rr[i] = ri[i] = 0.f;
+                    }
+                } else {
+                    const cx<float> a = tile[src];
+                    const float pr = t.rh * a.re - t.ih * a.im, pi = t.rh * a.im + t.ih * a.re;
+                    ar[i] += neg ? -pr : pr;
+                    ai[i] += neg ? -pi : pi;
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < NA; i++) {
+            const uint32_t u = threadIdx.x + 256u * (uint32_t)i;
+            const uint64_t gidx = base + chunk_off[u >> l] + (u & lowmask);
+            if (!p.init) {
+                const cx<float> o = lam[gidx];
+                ar[i] += o.re;
+                ai[i] += o.im;
+            }
+            lam[gidx] = cx<float>{ar[i], ai[i]};
+        }
+        __syncthreads();
+    }
+}
+
 // Re<a|b> of float-float states: per-thread float-float sums, then FP64.
 __global__ void __launch_bounds__(256) k_inner_re_ff(const ff2::v2 *__restrict__ a, const ff2::v2 *__restrict__ b,
                                                      uint64_t ns, double *partials, unsigned *ticket, double *result) {
@@ -802,7 +886,8 @@ static cudaError_t apply_hamiltonian(Sim &s, void *lam, const std::vector<ApplyG
 // The same passes on float-float resident states: each pass's strings are
 // ordered into runs of one coefficient (Z-type real, real with flips,
 // complex), the form k_apply_tile_ff sums.
-static cudaError_t apply_hamiltonian_tiled_ff(Sim &s, void *lam, const std::vector<PauliString> &H, bool &done) {
+static cudaError_t apply_hamiltonian_tiled_ff(Sim &s, void *lam, const std::vector<PauliString> &H, bool &done,
+                                              bool c64 = false) {
     done = false;
     const int K = kApplyTileBits;
     if (s.n < (uint32_t)K + 1 || H.empty()) return cudaSuccess;
@@ -811,9 +896,10 @@ static cudaError_t apply_hamiltonian_tiled_ff(Sim &s, void *lam, const std::vect
     std::vector<size_t> wide;
     const std::vector<PauliPass> passes = plan_pauli_passes(s.n, K, xm, kMaxTerms, wide);
     if (!wide.empty()) return cudaSuccess;
-    const size_t smem = (sizeof(ff2::v2) << K) + (sizeof(uint64_t) << (K - kLaneBits));
+    const size_t smem = ((c64 ? sizeof(cx<float>) : sizeof(ff2::v2)) << K) + (sizeof(uint64_t) << (K - kLaneBits));
     {
-        const cudaError_t e = ensure_smem_limit((const void *)k_apply_tile_ff, smem);
+        const cudaError_t e =
+            ensure_smem_limit(c64 ? (const void *)k_apply_tile_f32 : (const void *)k_apply_tile_ff, smem);
         if (e != cudaSuccess) return e;
     }
     const uint64_t tiles = 1ull << (s.n - K);
@@ -862,7 +948,10 @@ static cudaError_t apply_hamiltonian_tiled_ff(Sim &s, void *lam, const std::vect
             a.t[j] = items[j].t;
         }
         a.nterms = (uint32_t)items.size();
-        k_apply_tile_ff<<<grid, 256, smem, s.stream>>>((const ff2::v2 *)s.state, (ff2::v2 *)lam, s.n, a);
+        if (c64)
+            k_apply_tile_f32<<<grid, 256, smem, s.stream>>>((const cx<float> *)s.state, (cx<float> *)lam, s.n, a);
+        else
+            k_apply_tile_ff<<<grid, 256, smem, s.stream>>>((const ff2::v2 *)s.state, (ff2::v2 *)lam, s.n, a);
         count_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -1080,7 +1169,9 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         e = apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled);
         if (e == cudaSuccess && !tiled) e = apply_hamiltonian_ff(s, sc.lam, make_groups(H));
     } else {
-        e = apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
+        // (complex64: the run form of the float-float pass, in float)
+        e = sizeof(T) == 4 ? apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled, true)
+                           : apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
         if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, sc.lam, make_groups(H));
     }
     if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
