@@ -1169,9 +1169,10 @@ static int32_t adjoint_run(Sim &s, const std::vector<GateDesc> &fwd, const std::
         e = apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled);
         if (e == cudaSuccess && !tiled) e = apply_hamiltonian_ff(s, sc.lam, make_groups(H));
     } else {
-        // (complex64: the run form of the float-float pass, in float)
-        e = sizeof(T) == 4 ? apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled, true)
-                           : apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
+        if constexpr (sizeof(T) == 4)  // complex64: the run form of the float-float pass, in float
+            e = apply_hamiltonian_tiled_ff(s, sc.lam, H, tiled, true);
+        else
+            e = apply_hamiltonian_tiled<T>(s, sc.lam, H, tiled);
         if (e == cudaSuccess && !tiled) e = apply_hamiltonian<T>(s, sc.lam, make_groups(H));
     }
     if (e != cudaSuccess) return fail_cuda(e, "H|phi>");
