@@ -262,3 +262,24 @@ def test_batch_circuits_validation(lib):
     with pytest.raises(N.KbwgError) as e:
         batch_circuits_run(packed)
     assert e.value.code == N.EINVAL
+
+
+@pytest.mark.parametrize("prec,flags", [(N.C128, N.FLAG_FAST_C128), (N.C64, 0)])
+def test_specialised_kernels_above_32_qubits_compile(lib, prec, flags):
+    """Registers above 32 qubits: the specialised sweeps index with 64 bits
+    (controls and diagonal targets on qubits 32 and up compiled in as 64-bit
+    masks and shifts), and so do the specialised reverse sweeps of the
+    adjoint gradient; both compile for sm_103a (host only)."""
+    from kbw_gb300.dense import _gate_array
+    n = 34
+    circ = C.random_circuit(n, 90, 23, max_controls=2)
+    circ += [(C.RZ, 33, (), 0.4), (C.X, 2, (33, 32), 0.0), (C.P, 32, (1,), 0.9), (C.RY, 33, (32,), 0.3)]
+    try:
+        sweeps, failed = N.jit_check(n, prec, flags, _gate_array(circ))
+        assert sweeps > 0 and failed == 0, N.jit_last_error()
+        sweeps, failed = N.jit_check_adjoint(n, prec, flags, _gate_array(circ))
+        assert sweeps > 0 and failed == 0, N.jit_last_error()
+    except N.KbwgError as e:
+        if e.code == N.EUNSUPPORTED:
+            pytest.skip("NVRTC not available: %s" % e)
+        raise
