@@ -22,7 +22,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <exception>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -391,18 +393,32 @@ struct BatchCircuitIn {
     const char *error = nullptr;
 };
 
-// fn(i) for i in [0, n) on all host cores (items taken one at a time)
+// fn(i) for i in [0, n) on all host cores (items taken one at a time).  An
+// exception in any item (an allocation failing) stops the remaining items and
+// is rethrown here, on the calling thread, after every worker has joined.
 template <class F>
 static void batch_parallel_for(size_t n, F &&fn) {
     const size_t nt = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
     std::atomic<size_t> next{0};
+    std::mutex mu;
+    std::exception_ptr first;
     auto worker = [&]() {
-        for (size_t i; (i = next.fetch_add(1, std::memory_order_relaxed)) < n;) fn(i);
+        try {
+            for (size_t i; (i = next.fetch_add(1, std::memory_order_relaxed)) < n;) fn(i);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(mu);
+            if (!first) first = std::current_exception();
+            next.store(n);
+        }
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nt; t++) pool.emplace_back(worker);
+    try {
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(worker);
+    } catch (...) {  // fewer threads than asked: the ones started and this one share the items
+    }
     worker();
     for (std::thread &t : pool) t.join();
+    if (first) std::rethrow_exception(first);
 }
 
 template <class P, int K, int R>

@@ -27,6 +27,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <functional>
+#include <exception>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -204,20 +205,35 @@ int env_int(const char *name, int dflt) {
 
 const char *kClassName[] = {"TG_X", "TG_Y", "TG_H", "TG_RX", "TG_RY", "TG_Z", "TG_P", "TG_RZ", "TG_PI", "TG_SCALE"};
 
+// fn(w) for w in [0, count) on up to 32 threads.  An exception in an item
+// (an allocation failing) stops the remaining items and is rethrown on the
+// calling thread once every worker has joined.
 void run_parallel(size_t count, const std::function<void(size_t)> &fn, bool on_device = true) {
     const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
     const size_t nthreads = std::min<size_t>(count, std::min<size_t>(hw, 32));
     std::atomic<size_t> next{0};
     int dev = 0;
     const bool have_dev = on_device && cudaGetDevice(&dev) == cudaSuccess;
+    std::mutex emu;
+    std::exception_ptr first;
     auto worker = [&]() {
         if (have_dev) cudaSetDevice(dev);  // library loads happen on the caller's device
-        for (size_t w; (w = next.fetch_add(1)) < count;) fn(w);
+        try {
+            for (size_t w; (w = next.fetch_add(1)) < count;) fn(w);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(emu);
+            if (!first) first = std::current_exception();
+            next.store(count);
+        }
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nthreads; t++) pool.emplace_back(worker);
+    try {
+        for (size_t t = 1; t < nthreads; t++) pool.emplace_back(worker);
+    } catch (...) {  // fewer threads than asked: the ones started and this one share the items
+    }
     worker();
     for (std::thread &t : pool) t.join();
+    if (first) std::rethrow_exception(first);
 }
 
 }  // namespace
@@ -564,7 +580,7 @@ void stop_jobs() {
     for (std::thread &t : ts) t.join();
 }
 
-void run_job(std::shared_ptr<JitJob> job) {
+void run_job_body(const std::shared_ptr<JitJob> &job) {
     std::vector<size_t> todo;
     {
         std::lock_guard<std::mutex> lk(g_mu);
@@ -591,6 +607,17 @@ void run_job(std::shared_ptr<JitJob> job) {
             g_cubins.emplace(src, std::move(cubin));
         },
         false);
+}
+
+// A background job: its kernels compiled into the cubin cache.  Whatever
+// happens (an allocation failing), the job ends done, so that waiters return;
+// structures without a cubin then keep their interpreted kernels.
+void run_job(std::shared_ptr<JitJob> job) {
+    try {
+        run_job_body(job);
+    } catch (...) {
+        note_error("background compilation stopped: host allocation failed");
+    }
     {
         std::lock_guard<std::mutex> lk(job->mu);
         job->srcs.clear();  // the cubins are in the cache; the sources are no longer needed
