@@ -359,8 +359,8 @@ std::string jit_sweep_source(const JitGeometry &geo, const PlannedSweep &sw) {
     std::string s;
     s.reserve(4096 + 160 * sw.gates.size());
     char buf[512];
-    const int first = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.front();
-    const int last = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.back();
+    const int first = sw.stage_layout.empty() ? (int)LAYOUT_A : (int)sw.stage_layout.front();
+    const int last = sw.stage_layout.empty() ? (int)LAYOUT_A : (int)sw.stage_layout.back();
     s += "#include \"jit_dev.cuh\"\n"
          "using namespace kbwg;\n"
          "namespace {\n";
@@ -404,8 +404,8 @@ std::string jit_adjoint_source(const JitGeometry &geo, const PlannedSweep &sw, c
     std::string s;
     s.reserve(4096 + 320 * sw.gates.size());
     char buf[512];
-    const int first = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.front();
-    const int last = sw.stage_layout.empty() ? LAYOUT_A : sw.stage_layout.back();
+    const int first = sw.stage_layout.empty() ? (int)LAYOUT_A : (int)sw.stage_layout.front();
+    const int last = sw.stage_layout.empty() ? (int)LAYOUT_A : (int)sw.stage_layout.back();
     s += "#include \"adjoint_dev.cuh\"\n"
          "using namespace kbwg;\n"
          "namespace {\n"
