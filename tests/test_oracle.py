@@ -150,12 +150,29 @@ def test_golden_fixtures_regenerate(tmp_path):
             assert np.allclose(a[k], b[k], rtol=0, atol=1e-13), (f, k)
 
 
-def _densev2_apply(re, im, n, gate):
-    """One gate in DenseV2's in-place form (src/dense_v2.rs:166-280), in
-    numpy binary64 with its own expressions: pairs (ket0, ket1) split at the
-    target bit, complex products as num's Mul (re*re' - im*im', re*im' +
-    im*re'), constants from libm through Python's math module."""
+def _libm_f32():
+    import ctypes
+    import ctypes.util
+    m = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+    for f in ("cosf", "sinf"):
+        getattr(m, f).restype = ctypes.c_float
+        getattr(m, f).argtypes = [ctypes.c_float]
+    return m
+
+
+def _densev2_apply(re, im, n, gate, f32=None):
+    """One gate in DenseV2's in-place form (src/dense_v2.rs:166-280) with its
+    own expressions, in numpy binary64 or (f32: libm handle) binary32: pairs
+    (ket0, ket1) split at the target bit, complex products as num's Mul
+    (re*re' - im*im', re*im' + im*re'), constants from libm (cos/sin through
+    Python's math module; cosf/sinf of the binary32 angle)."""
     kind, t, ctrl, a = gate
+    if f32 is None:
+        T, cos, sin = float, math.cos, math.sin
+    else:
+        T = np.float32
+        cos = lambda x: np.float32(f32.cosf(float(np.float32(x))))  # noqa: E731
+        sin = lambda x: np.float32(f32.sinf(float(np.float32(x))))  # noqa: E731
     idx = np.arange(1 << n)
     mask = 0
     for c in ctrl:
@@ -170,45 +187,47 @@ def _densev2_apply(re, im, n, gate):
     if kind == C.X:
         re[i0], im[i0], re[i1], im[i1] = r1, m1, r0, m0
     elif kind == C.Y:  # swap, then ket0 *= -i, ket1 *= i
-        re[i0], im[i0] = cmul(r1, m1, -0.0, -1.0)
-        re[i1], im[i1] = cmul(r0, m0, 0.0, 1.0)
+        re[i0], im[i0] = cmul(r1, m1, T(-0.0), T(-1.0))
+        re[i1], im[i1] = cmul(r0, m0, T(0.0), T(1.0))
     elif kind == C.Z:  # ket1 *= -1
-        re[i1], im[i1] = cmul(r1, m1, -1.0, -0.0)
+        re[i1], im[i1] = cmul(r1, m1, T(-1.0), T(-0.0))
     elif kind == C.H:
-        s = 0.70710678118654752440
+        s = T(0.70710678118654752440)
         re[i0], im[i0] = (r0 + r1) * s, (m0 + m1) * s
         re[i1], im[i1] = (r0 - r1) * s, (m0 - m1) * s
     elif kind == C.P:  # ket1 *= exp(i lambda)
-        re[i1], im[i1] = cmul(r1, m1, math.cos(a), math.sin(a))
+        re[i1], im[i1] = cmul(r1, m1, cos(a), sin(a))
     elif kind == C.RX:
-        c, s = math.cos(a / 2.0), math.sin(a / 2.0)
+        c, s = cos(a / 2.0), sin(a / 2.0)
         re[i0], im[i0] = c * r0 + s * m1, c * m0 - s * r1
         re[i1], im[i1] = s * m0 + c * r1, -s * r0 + c * m1
     elif kind == C.RY:
-        c, s = math.cos(a / 2.0), math.sin(a / 2.0)
+        c, s = cos(a / 2.0), sin(a / 2.0)
         re[i0], im[i0] = c * r0 - s * r1, c * m0 - s * m1
         re[i1], im[i1] = s * r0 + c * r1, s * m0 + c * m1
     else:  # RZ: ket0 *= exp(-i theta/2), ket1 *= exp(i theta/2)
         h0, h1 = -a / 2.0, a / 2.0
-        re[i0], im[i0] = cmul(r0, m0, math.cos(h0), math.sin(h0))
-        re[i1], im[i1] = cmul(r1, m1, math.cos(h1), math.sin(h1))
+        re[i0], im[i0] = cmul(r0, m0, cos(h0), sin(h0))
+        re[i1], im[i1] = cmul(r1, m1, cos(h1), sin(h1))
 
 
-@pytest.mark.parametrize("seed", [5, 6])
-def test_densev2_formulas_equal_the_dense_restatement(seed):
+@pytest.mark.parametrize("seed,prec", [(5, "c128"), (6, "c128"), (7, "c64")])
+def test_densev2_formulas_equal_the_dense_restatement(seed, prec):
     """The C ABI's default simulator is DenseV2 (in place); the oracle
     restates Dense (double-buffered).  Their gate bodies compute the same
     products and two-term sums up to order and exact negations, so DenseV2's
     amplitudes are the oracle's bit for bit: checked on random circuits with
-    every gate kind and controls."""
+    every gate kind and controls, in binary64 and binary32."""
     n = 9
     circ = C.random_circuit(n, 400, seed, max_controls=2)
-    re = np.zeros(1 << n)
-    im = np.zeros(1 << n)
+    f32 = _libm_f32() if prec == "c64" else None
+    dt = np.float32 if f32 else np.float64
+    re = np.zeros(1 << n, dt)
+    im = np.zeros(1 << n, dt)
     re[0] = 1.0
     for g in circ:
-        _densev2_apply(re, im, n, g)
-    o = oracle.OracleDense(n, "c128")
+        _densev2_apply(re, im, n, g, f32)
+    o = oracle.OracleDense(n, prec)
     o.apply(circ)
     st = o.state()
     assert np.array_equal(st.real, re) and np.array_equal(st.imag, im)
