@@ -16,7 +16,15 @@ is cleared, every gate is submitted by its own trait call, then <Z_i> for all
 qubits and one full-register measurement (host draws) are read back.
 Before the warm-up the engine's autotuner times the compiled tile sizes and
 fusion depths on the circuit and keeps the fastest (config.tuning;
---no-tune keeps the defaults).
+--no-tune keeps the defaults).  The fused sweeps apply ~50 gates each in
+float-float arithmetic and are bound by FP32-pipe issue, not HBM, so the
+roofline fraction of a fused launch is low while the step is fast; the
+single_gate_sweep line shows the HBM roof of a one-gate sweep.
+
+--impl reference: the reference's CPU Dense path as the restated Dense<f64>
+(oracle/, OpenMP on every host core) on the same circuit: the timed steps
+apply the whole 890-gate circuit once between them (--ref-gates G: G gates
+per step instead), same metric and unit.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
