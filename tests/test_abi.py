@@ -283,3 +283,39 @@ def test_specialised_kernels_above_32_qubits_compile(lib, prec, flags):
         if e.code == N.EUNSUPPORTED:
             pytest.skip("NVRTC not available: %s" % e)
         raise
+
+
+@pytest.mark.parametrize("n,prec,fast", [(33, "c128", True), (36, "c64", False), (40, "c128", False)])
+def test_planner_wide_registers(lib, n, prec, fast):
+    """Registers above 32 qubits, where no state fits the oracle: the
+    planner places every gate once, keeps each non-diagonal gate's target in
+    its sweep's tile, and never swaps two gates that share a qubit on which
+    either acts non-diagonally (controls and diagonal targets commute)."""
+    from kbw_gb300.dense import plan
+    rng = np.random.default_rng(n)
+    circ = C.random_circuit(n, 220, int(rng.integers(0, 1 << 30)), max_controls=3)
+    circ += [(C.RZ, n - 1, (), 0.3), (C.X, 0, (n - 1, n - 2), 0.0), (C.H, n - 1, (5,), 0.0),
+             (C.P, n - 3, (n - 1,), 0.7), (C.RY, 31, (n - 1,), 0.2), (C.RX, n - 2, (), 0.4)]
+    diag = {C.Z, C.P, C.RZ}
+    sweeps = plan(n, circ, prec, fast_c128=fast)
+    order = [i for _, idx in sweeps for i in idx]
+    assert sorted(order) == list(range(len(circ)))
+    pos = {g: k for k, g in enumerate(order)}
+    for mask, idx in sweeps:
+        for i in idx:
+            kind, t, c, a = circ[i]
+            if kind not in diag:
+                assert mask >> t & 1, (i, t, hex(mask))
+
+    def acts(g):  # qubit -> True if the gate acts on it non-diagonally
+        kind, t, c, a = g
+        out = {q: False for q in c}
+        out[t] = kind not in diag
+        return out
+
+    for i in range(len(circ)):
+        ai = acts(circ[i])
+        for j in range(i + 1, len(circ)):
+            aj = acts(circ[j])
+            if any(q in aj and (ai[q] or aj[q]) for q in ai):
+                assert pos[i] < pos[j], (i, j, circ[i], circ[j])
